@@ -1,0 +1,151 @@
+/*
+ * teufel_cuda.h -- C-ABI of the GB300 (sm_103a) Lienard-Wiechert field
+ * integration for TEUFEL observers.
+ *
+ * This is the drop-in boundary for TEUFEL's field-integration step.  In the
+ * reference the step is reached through the observer API:
+ *
+ *   BaseObserver::integrate()                     src/observer.h:55
+ *     ScreenObserver<Beam>::integrate()           src/screen.cpp:113-146
+ *     MeshedScreen<Beam>::integrate()             src/mesh.cpp:289-316
+ *     PointObserver<Beam>::integrate()            src/point_observer.cpp:62-66
+ *   -> Beam::integrateFieldTrace                  src/beam.cpp:443-451
+ *   -> Bunch::integrateFieldTrace                 src/bunch.cpp:739-745
+ *   -> ChargedParticle::integrateFieldTrace       src/particle.cpp:771-867
+ *
+ * and the traces leave through getBuffer() as [pixel][sample][Ex,Ey,Ez,Bx,By,Bz]
+ * doubles (src/screen.cpp:249-272, src/mesh.cpp:376-399,
+ * src/point_observer.cpp:78-89).  The functions below replace the body of
+ * those integrate() specialisations: the caller passes the observation points
+ * and per-point trace start times it already holds, and receives the traces
+ * in that same buffer layout, accumulated (+=) into what the buffer holds, as
+ * FieldTrace::add accumulates into traces that zero() cleared.
+ *
+ * Conventions
+ *  - Plain C types only; every function returns a status code (TEUFEL_OK = 0)
+ *    and never throws.  teufel_cuda_status_string() gives a message.
+ *  - Trajectories are uploaded once (teufel_cuda_traj_upload) and stay
+ *    resident on the device across observers until teufel_cuda_traj_free.
+ *  - Calls are asynchronous on the given stream internally and synchronous at
+ *    return for host buffers; the *_ex entry with device pointers returns once
+ *    the work is enqueued.
+ *  - A handle is not re-entrant: one call at a time per teufel_traj_set.
+ */
+#ifndef TEUFEL_CUDA_H
+#define TEUFEL_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TEUFEL_OK 0
+#define TEUFEL_ERR_ARG 1      /* bad argument: null pointer, negative size, non-finite value */
+#define TEUFEL_ERR_NOMEM 2    /* device or pinned-host allocation failed */
+#define TEUFEL_ERR_CUDA 3     /* a CUDA runtime call failed */
+#define TEUFEL_ERR_RANGE 4    /* a deposit fell outside its trace: the condition on which
+                                 FieldTrace::add throws IOexception (src/fieldtrace.cpp:185-190);
+                                 the offending deposit is skipped, all others are kept */
+#define TEUFEL_ERR_NODEVICE 6 /* no CUDA device, or not an sm_103 device */
+
+/* ---- arithmetic of the integration -------------------------------------- */
+#define TEUFEL_PREC_FP32_SPLIT 0 /* FP32 fields with split-form 1-n.beta; FP64 anchors,
+                                    bin indices bit-identical to the reference */
+#define TEUFEL_PREC_FP64 1       /* plain FP64 throughout, in the reference's operation order */
+
+typedef struct teufel_traj_set teufel_traj_set; /* opaque, device-resident */
+typedef void *teufel_stream_t;                   /* a cudaStream_t; NULL = default stream */
+
+typedef struct teufel_options {
+    int precision;        /* TEUFEL_PREC_*                                        */
+    int device_pointers;  /* 1: pix_pos, pix_t0 and out are device pointers      */
+    int n_slots;          /* particle-range slots reduced in FP64; 0 = automatic  */
+    int threads_per_block;/* 0 = automatic (128)                                 */
+} teufel_options;
+
+/* Fill *opt with the defaults (FP32 split path, host pointers, automatic tiling). */
+void teufel_cuda_default_options(teufel_options *opt);
+
+/* Message for a status code. */
+const char *teufel_cuda_status_string(int status);
+
+/* Upload the trajectories of a particle set and keep them resident.
+ * Replaces the per-pixel reads of ChargedParticle::Time/X/P/A
+ * (src/particle.h:417-427) made by integrateFieldTrace.
+ *   n_particles          number of particles (>= 0)
+ *   n_points[n]          trajectory points per particle (NP, src/particle.h:378)
+ *   charge_e[n]          ChargedParticle::Charge, in units of e (src/particle.h:388)
+ *   t[Npts]              trajectory times [s], Npts = sum(n_points), particles concatenated
+ *   x[Npts][3]           positions [m]
+ *   bg[Npts][3]          beta*gamma (TrajMomentum)
+ *   a[Npts][3]           d(beta*gamma)/dt [1/s] (TrajAccel)
+ * Non-finite inputs are rejected with TEUFEL_ERR_ARG. */
+int teufel_cuda_traj_upload(int n_particles, const int *n_points, const double *charge_e,
+                            const double *t, const double *x, const double *bg, const double *a,
+                            teufel_traj_set **out);
+
+/* Release a trajectory set and its device memory.  NULL is accepted. */
+int teufel_cuda_traj_free(teufel_traj_set *traj);
+
+/* Total trajectory points held by the set (for sizing and diagnostics). */
+int64_t teufel_cuda_traj_points(const teufel_traj_set *traj);
+
+/* Integrate the fields of all particles onto Np observation points.
+ * Replaces MeshedScreen<Beam>::integrate (src/mesh.cpp:289-316) and
+ * ScreenObserver<Beam>::integrate (src/screen.cpp:113-146): pixel i observes
+ * at pix_pos[i] with trace t0 = pix_t0[i], step dt, Nt samples; the result is
+ * added into out[Np][Nt][6] (host memory).  Nt < 2 or an empty particle set
+ * leaves out unchanged, as the reference does (src/particle.cpp:778-783). */
+int teufel_cuda_integrate_screen(const teufel_traj_set *traj, const double *pix_pos,
+                                 const double *pix_t0, double dt, int Nt, int Np, double *out,
+                                 teufel_stream_t s);
+
+/* One observation point: replaces PointObserver<Beam>::integrate
+ * (src/point_observer.cpp:62-66).  out[Nt][6] (host memory) is added into. */
+int teufel_cuda_integrate_point(const teufel_traj_set *traj, const double *pos, double t0,
+                                double dt, int Nt, double *out, teufel_stream_t s);
+
+/* As teufel_cuda_integrate_screen, with explicit options (precision, device
+ * pointers for pix_pos/pix_t0/out, tiling).  With device pointers the call
+ * returns once the work is enqueued on s. */
+int teufel_cuda_integrate_screen_ex(const teufel_traj_set *traj, const double *pix_pos,
+                                    const double *pix_t0, double dt, int Nt, int Np, double *out,
+                                    const teufel_options *opt, teufel_stream_t s);
+
+/* ---- diagnostics used by the parity tests and the benchmark -------------- */
+
+/* Per trajectory point of particle m, as observed from pos with a trace
+ * (t0, dt, Nt), the decision the device path takes: the bin index
+ * round((ts-t0)/dt) clamped to [-2, Nt+1], flags bit0 = (ts <= tmin),
+ * bit1 = (ts < tmax), bit2 = resolved by the exact FP64 fallback; and u_est,
+ * the FP32-path estimate of (ts-t0)/dt.  The same device functions as the
+ * main FP32 kernel are used.  Arrays have n_points[m] entries (host memory). */
+int teufel_cuda_point_decisions(const teufel_traj_set *traj, int m, const double *pos, double t0,
+                                double dt, int Nt, int64_t *idx, int *flags, double *u_est);
+
+/* Run the device deposit routine on injected arrival times and fields (the
+ * reference's known-answer test, tests/teufel.integrate_field.cpp:51-78,
+ * injects them by overriding RetardedTime/RetardedField).  n_points[n],
+ * ts[Npts], f[Npts][6] (host).  precision selects the FP64 or FP32 deposit.
+ * trace[Nt][6] (host) is added into. */
+int teufel_cuda_deposit_injected(int n_particles, const int *n_points, const double *ts,
+                                 const double *f, double t0, double dt, int Nt, int precision,
+                                 double *trace);
+
+/* In-window step count of the last integrate call on this handle: the
+ * number of (pixel, particle, step) triples whose arrival interval overlapped
+ * the trace window (the reference's condition at src/particle.cpp:793). */
+int teufel_cuda_last_inwindow(const teufel_traj_set *traj, int64_t *inwindow,
+                              int64_t *fallback_points);
+
+/* Peak FP32 FMA throughput of the current device measured with a dependent-
+ * free FFMA kernel (TFLOP/s, FMA = 2 flops), and the same for FP64 DFMA. */
+int teufel_cuda_probe_peaks(double *fp32_tflops, double *fp64_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TEUFEL_CUDA_H */

@@ -1,0 +1,208 @@
+"""Parity of the CUDA field integration (through the C-ABI) with the CPU
+oracle, which is pinned to the reference by tests/test_oracle_*.py.
+
+Bars: bin indices and window decisions bit-identical to the reference for
+both precisions; FP64 device traces within 1e-12 relative L2 of the oracle;
+FP32-split traces within 1e-5 relative L2 (the target the split path is
+specified to), plus a per-pixel check on the strong pixels."""
+import numpy as np
+import pytest
+
+from oracle import lw
+from teufel_gb300 import abi, harness as H
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12
+TOL_FP32 = 1e-5
+
+
+def rel_l2(a, b):
+    n = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / n if n > 0 else np.linalg.norm(a - b)
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return H.config1()
+
+
+@pytest.fixture(scope="module")
+def c1_oracle(c1):
+    out, rc = lw.integrate_screen(c1.traj, c1.pix_pos, c1.pix_t0, c1.dt, c1.nots)
+    assert rc == 0
+    return out
+
+
+# ---------------------------------------------------------------- KAT ----
+from test_oracle_kat import KAT, kat_inputs  # noqa: E402
+
+
+@pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_FP32_SPLIT])
+@pytest.mark.parametrize("case", range(len(KAT)))
+def test_device_deposit_kat(case, prec):
+    parts, t0, dt, n, expect = KAT[case]
+    ts, fs = kat_inputs(parts)
+    tr, st = abi.deposit_injected(ts, fs, t0, dt, n, precision=prec)
+    assert st == 0
+    np.testing.assert_allclose(tr[:, 0], expect, atol=1e-6, rtol=0)
+    if prec == abi.PREC_FP64:
+        ref, _ = lw.deposit_injected(ts, fs, t0, dt, n)
+        assert np.array_equal(tr, ref)
+
+
+def test_device_deposit_range_errors():
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "range_error.npz"))
+    nots = int(g["nots"])
+    f = [[[1.0, 2.0, 3.0, 4.0, 5.0, 6.0], [2.0, 3.0, 4.0, 5.0, 6.0, 7.0]]]
+    for (t0, dt, a, b), st, ref in zip(g["cases"], g["status"], g["traces"]):
+        tr, rc = abi.deposit_injected([[a, b]], f, t0, dt, nots, precision=abi.PREC_FP64)
+        assert rc == st
+        np.testing.assert_allclose(tr, ref, rtol=1e-15, atol=0)
+
+
+# ------------------------------------------------------------ config 1 ----
+def test_config1_fp64_matches_oracle(c1, c1_oracle):
+    with abi.TrajSet(c1.traj) as ts:
+        g = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots, precision=abi.PREC_FP64)
+        inwin, _, st = ts.last_inwindow()
+    assert st == 0
+    assert rel_l2(g, c1_oracle) < TOL_FP64
+    # same set of touched bins
+    assert np.array_equal(g != 0, c1_oracle != 0)
+    assert inwin > 0
+
+
+def test_config1_fp32_matches_oracle(c1, c1_oracle):
+    with abi.TrajSet(c1.traj) as ts:
+        g = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots)
+        inwin, fb, st = ts.last_inwindow()
+    assert st == 0
+    e = rel_l2(g, c1_oracle)
+    assert e < TOL_FP32, e
+    assert np.array_equal(g != 0, c1_oracle != 0)
+
+
+def test_config1_bin_indices_bit_exact(c1):
+    """Every point's bin index and window flags, as decided by the device
+    FP32 path (with its exact fallback), equal the reference arithmetic's."""
+    rng = np.random.default_rng(1)
+    with abi.TrajSet(c1.traj) as ts:
+        for p in rng.choice(c1.n_pix, 24, replace=False):
+            idx, flags, u = ts.point_decisions(0, c1.pix_pos[p], c1.pix_t0[p], c1.dt, c1.nots)
+            ri, rf = lw.point_decisions(c1.traj, 0, c1.pix_pos[p], c1.pix_t0[p], c1.dt, c1.nots)
+            assert np.array_equal(idx, ri)
+            assert np.array_equal(flags & 3, rf)
+
+
+def test_config1_point_observer(c1, c1_oracle):
+    p = c1.n_pix // 2
+    with abi.TrajSet(c1.traj) as ts:
+        g = ts.integrate_point(c1.pix_pos[p], c1.pix_t0[p], c1.dt, c1.nots)
+    assert rel_l2(g, c1_oracle[p]) < TOL_FP32
+
+
+def test_accumulates_into_out(c1, c1_oracle):
+    sel = np.arange(0, c1.n_pix, 9)
+    base = np.random.default_rng(3).normal(size=(len(sel), c1.nots, 6))
+    with abi.TrajSet(c1.traj) as ts:
+        g = ts.integrate_screen(c1.pix_pos[sel], c1.pix_t0[sel], c1.dt, c1.nots, out=base.copy(),
+                                precision=abi.PREC_FP64)
+    np.testing.assert_allclose(g - base, c1_oracle[sel], rtol=0, atol=1e-12 *
+                               np.abs(c1_oracle).max())
+
+
+def test_deterministic(c1):
+    with abi.TrajSet(c1.traj) as ts:
+        a = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots)
+        b = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots)
+    assert np.array_equal(a, b)
+
+
+# ------------------------------------------------------ bunch subsets ----
+def _bunch_case(cfg, count, pix_step):
+    w = cfg(count=count)
+    sel = np.arange(0, w.n_pix, pix_step)
+    return w.pixel_subset(sel)
+
+
+@pytest.mark.parametrize("name,cfg,count,pix_step", [
+    ("config2", H.config2, 48, 37),
+    ("config4", H.config4, 6, 613),
+    ("config5", H.config5, 6, 127),
+])
+def test_bunch_subset_parity(name, cfg, count, pix_step):
+    w = _bunch_case(cfg, count, pix_step)
+    ref, rc = lw.integrate_screen(w.traj, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rc == 0
+    assert np.abs(ref).max() > 0
+    with abi.TrajSet(w.traj) as ts:
+        g64 = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=abi.PREC_FP64)
+        g32 = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots)
+        _, fb, st = ts.last_inwindow()
+        assert st == 0
+        # bin decisions on a few (pixel, particle) pairs
+        for p in range(0, w.n_pix, max(1, w.n_pix // 5)):
+            for m in range(0, count, max(1, count // 2)):
+                idx, flags, _ = ts.point_decisions(m, w.pix_pos[p], w.pix_t0[p], w.dt, w.nots)
+                ri, rf = lw.point_decisions(w.traj, m, w.pix_pos[p], w.pix_t0[p], w.dt, w.nots)
+                assert np.array_equal(idx, ri)
+                assert np.array_equal(flags & 3, rf)
+    assert rel_l2(g64, ref) < TOL_FP64
+    e = rel_l2(g32, ref)
+    assert e < TOL_FP32, (name, e)
+
+
+def test_charge_linearity(c1):
+    """Doubling every charge doubles every trace sample exactly."""
+    tr = c1.traj
+    tr2 = H.Trajectories(tr.t, tr.x, tr.p, tr.a, tr.n_points, tr.charge * 2.0, tr.mass)
+    sel = np.arange(0, c1.n_pix, 5)
+    with abi.TrajSet(tr) as a, abi.TrajSet(tr2) as b:
+        for prec in (abi.PREC_FP32_SPLIT, abi.PREC_FP64):
+            ga = a.integrate_screen(c1.pix_pos[sel], c1.pix_t0[sel], c1.dt, c1.nots,
+                                    precision=prec)
+            gb = b.integrate_screen(c1.pix_pos[sel], c1.pix_t0[sel], c1.dt, c1.nots,
+                                    precision=prec)
+            assert np.array_equal(2.0 * ga, gb)
+
+
+# ----------------------------------------------------------- edge cases --
+def test_short_trace_and_empty_inputs(c1):
+    with abi.TrajSet(c1.traj) as ts:
+        out = np.ones((3, 1, 6))
+        ts.integrate_screen(c1.pix_pos[:3], c1.pix_t0[:3], c1.dt, 1, out=out)
+        assert np.all(out == 1.0)  # nots < 2: nothing happens (src/particle.cpp:778)
+        out = np.zeros((0, 16, 6))
+        ts.integrate_screen(np.zeros((0, 3)), np.zeros(0), c1.dt, 16, out=out)
+    empty = H.Trajectories(np.zeros(0), np.zeros((0, 3)), np.zeros((0, 3)), np.zeros((0, 3)),
+                           np.zeros(0, np.int32), np.zeros(0), np.zeros(0))
+    with abi.TrajSet(empty) as ts:
+        out = np.zeros((2, 8, 6))
+        ts.integrate_screen(c1.pix_pos[:2], c1.pix_t0[:2], c1.dt, 8, out=out)
+        assert np.all(out == 0.0)
+
+
+def test_single_point_particles_are_skipped(c1):
+    tr = c1.traj
+    one = H.Trajectories(np.concatenate([tr.t[:1], tr.t]), np.concatenate([tr.x[:1], tr.x]),
+                         np.concatenate([tr.p[:1], tr.p]), np.concatenate([tr.a[:1], tr.a]),
+                         np.array([1, tr.n_points[0]], np.int32), np.array([-1.0, -1.0]),
+                         np.array([1.0, 1.0]))
+    sel = np.arange(0, c1.n_pix, 20)
+    ref, _ = lw.integrate_screen(one, c1.pix_pos[sel], c1.pix_t0[sel], c1.dt, c1.nots)
+    with abi.TrajSet(one) as ts:
+        g = ts.integrate_screen(c1.pix_pos[sel], c1.pix_t0[sel], c1.dt, c1.nots,
+                                precision=abi.PREC_FP64)
+    assert rel_l2(g, ref) < TOL_FP64
+
+
+def test_non_finite_trajectory_rejected(c1):
+    tr = c1.traj
+    bad = H.Trajectories(tr.t.copy(), tr.x.copy(), tr.p.copy(), tr.a.copy(), tr.n_points,
+                         tr.charge, tr.mass)
+    bad.x[17, 1] = np.nan
+    with pytest.raises(abi.TeufelError) as ei:
+        abi.TrajSet(bad)
+    assert ei.value.status == abi.TEUFEL_ERR_ARG

@@ -1,0 +1,251 @@
+"""ctypes binding of the C-ABI in include/teufel_cuda.h (libteufel_gb300.so).
+
+The library is built in-tree (teufel_gb300/_lib) on first use.  There is no
+CPU fallback: without the CUDA library or an sm_103 device the calls return
+TEUFEL_ERR_NODEVICE and the Python wrappers raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import _build
+
+TEUFEL_OK = 0
+TEUFEL_ERR_ARG = 1
+TEUFEL_ERR_NOMEM = 2
+TEUFEL_ERR_CUDA = 3
+TEUFEL_ERR_RANGE = 4
+TEUFEL_ERR_NODEVICE = 6
+
+PREC_FP32_SPLIT = 0
+PREC_FP64 = 1
+
+# The functions include/teufel_cuda.h declares (checked by the tests).
+EXPORTED = [
+    "teufel_cuda_default_options", "teufel_cuda_status_string", "teufel_cuda_traj_upload",
+    "teufel_cuda_traj_free", "teufel_cuda_traj_points", "teufel_cuda_integrate_screen",
+    "teufel_cuda_integrate_point", "teufel_cuda_integrate_screen_ex",
+    "teufel_cuda_point_decisions", "teufel_cuda_deposit_injected", "teufel_cuda_last_inwindow",
+    "teufel_cuda_probe_peaks",
+]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("device_pointers", ctypes.c_int),
+                ("n_slots", ctypes.c_int), ("threads_per_block", ctypes.c_int)]
+
+
+class TeufelError(RuntimeError):
+    """A non-zero status of the C-ABI.  TEUFEL_ERR_RANGE corresponds to the
+    IOexception that FieldTrace::add throws (src/fieldtrace.cpp:185-190)."""
+
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = status_string(status)
+        super().__init__(f"{what}: {msg} (status {status})" if what else msg)
+
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_cuda()
+        if not os.path.exists(path):
+            raise RuntimeError(f"CUDA library missing: {path}")
+        L = ctypes.CDLL(str(path))
+        L.teufel_cuda_default_options.restype = None
+        L.teufel_cuda_default_options.argtypes = [ctypes.POINTER(Options)]
+        L.teufel_cuda_status_string.restype = ctypes.c_char_p
+        L.teufel_cuda_status_string.argtypes = [ctypes.c_int]
+        L.teufel_cuda_traj_upload.restype = ctypes.c_int
+        L.teufel_cuda_traj_upload.argtypes = [ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp,
+                                              ctypes.POINTER(_vp)]
+        L.teufel_cuda_traj_free.restype = ctypes.c_int
+        L.teufel_cuda_traj_free.argtypes = [_vp]
+        L.teufel_cuda_traj_points.restype = ctypes.c_int64
+        L.teufel_cuda_traj_points.argtypes = [_vp]
+        L.teufel_cuda_integrate_screen.restype = ctypes.c_int
+        L.teufel_cuda_integrate_screen.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int,
+                                                   ctypes.c_int, _vp, _vp]
+        L.teufel_cuda_integrate_point.restype = ctypes.c_int
+        L.teufel_cuda_integrate_point.argtypes = [_vp, _dp, ctypes.c_double, ctypes.c_double,
+                                                  ctypes.c_int, _dp, _vp]
+        L.teufel_cuda_integrate_screen_ex.restype = ctypes.c_int
+        L.teufel_cuda_integrate_screen_ex.argtypes = [_vp, _vp, _vp, ctypes.c_double,
+                                                      ctypes.c_int, ctypes.c_int, _vp,
+                                                      ctypes.POINTER(Options), _vp]
+        L.teufel_cuda_point_decisions.restype = ctypes.c_int
+        L.teufel_cuda_point_decisions.argtypes = [_vp, ctypes.c_int, _dp, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_int, _lp, _ip, _dp]
+        L.teufel_cuda_deposit_injected.restype = ctypes.c_int
+        L.teufel_cuda_deposit_injected.argtypes = [ctypes.c_int, _ip, _dp, _dp, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                                   _dp]
+        L.teufel_cuda_last_inwindow.restype = ctypes.c_int
+        L.teufel_cuda_last_inwindow.argtypes = [_vp, _lp, _lp]
+        L.teufel_cuda_probe_peaks.restype = ctypes.c_int
+        L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp]
+        _lib = L
+    return _lib
+
+
+def status_string(status: int) -> str:
+    return lib().teufel_cuda_status_string(status).decode()
+
+
+def check(status: int, what: str = "") -> None:
+    if status != TEUFEL_OK:
+        raise TeufelError(status, what)
+
+
+def _c(a, dtype=np.float64):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
+            n_slots: int = 0) -> Options:
+    o = Options()
+    lib().teufel_cuda_default_options(ctypes.byref(o))
+    o.precision = precision
+    o.device_pointers = 1 if device_pointers else 0
+    o.n_slots = n_slots
+    return o
+
+
+class TrajSet:
+    """A device-resident particle set (teufel_cuda_traj_upload)."""
+
+    def __init__(self, traj):
+        L = lib()
+        n = traj.n_particles
+        npnt = _c(traj.n_points, np.int32)
+        ch = _c(traj.charge)
+        t, x, p, a = _c(traj.t), _c(traj.x), _c(traj.p), _c(traj.a)
+        h = _vp()
+        check(L.teufel_cuda_traj_upload(n, _ptr(npnt, _ip), _ptr(ch), _ptr(t), _ptr(x), _ptr(p),
+                                        _ptr(a), ctypes.byref(h)), "teufel_cuda_traj_upload")
+        self.handle = h
+        self.n_particles = n
+        self.n_points = npnt.copy()
+
+    @classmethod
+    def from_arrays(cls, n_points, charge, t, x, p, a):
+        """Upload from raw pointers-compatible arrays (host, possibly pinned)."""
+        class _T:
+            pass
+        tr = _T()
+        tr.n_particles = len(n_points)
+        tr.n_points, tr.charge, tr.t, tr.x, tr.p, tr.a = n_points, charge, t, x, p, a
+        return cls(tr)
+
+    def free(self):
+        if self.handle:
+            lib().teufel_cuda_traj_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    def points(self) -> int:
+        return int(lib().teufel_cuda_traj_points(self.handle))
+
+    # -- integration ----------------------------------------------------
+    def integrate_screen(self, pix_pos, pix_t0, dt, nots, out=None,
+                         precision: int = PREC_FP32_SPLIT, n_slots: int = 0,
+                         stream: int = 0) -> np.ndarray:
+        """Traces of all particles on the pixels, added into ``out``
+        ([Np][nots][6] doubles, zeros if None) -- host buffers."""
+        pix_pos = _c(pix_pos).reshape(-1, 3)
+        pix_t0 = _c(pix_t0).reshape(-1)
+        n_pix = pix_pos.shape[0]
+        if out is None:
+            out = np.zeros((n_pix, nots, 6))
+        if not (out.dtype == np.float64 and out.flags.c_contiguous):
+            raise ValueError("out must be a C-contiguous float64 array")
+        opt = options(precision, False, n_slots)
+        check(lib().teufel_cuda_integrate_screen_ex(self.handle, pix_pos.ctypes.data,
+                                                    pix_t0.ctypes.data, dt, nots, n_pix,
+                                                    out.ctypes.data, ctypes.byref(opt),
+                                                    _vp(stream)),
+              "teufel_cuda_integrate_screen")
+        return out
+
+    def integrate_screen_device(self, pos_ptr: int, t0_ptr: int, dt: float, nots: int,
+                                n_pix: int, out_ptr: int, precision: int = PREC_FP32_SPLIT,
+                                n_slots: int = 0, stream: int = 0) -> None:
+        """Device-pointer variant; returns once the work is enqueued."""
+        opt = options(precision, True, n_slots)
+        check(lib().teufel_cuda_integrate_screen_ex(self.handle, _vp(pos_ptr), _vp(t0_ptr), dt,
+                                                    nots, n_pix, _vp(out_ptr),
+                                                    ctypes.byref(opt), _vp(stream)),
+              "teufel_cuda_integrate_screen_ex")
+
+    def integrate_point(self, pos, t0, dt, nots, out=None) -> np.ndarray:
+        pos = _c(pos).reshape(3)
+        if out is None:
+            out = np.zeros((nots, 6))
+        check(lib().teufel_cuda_integrate_point(self.handle, _ptr(pos), t0, dt, nots, _ptr(out),
+                                                None), "teufel_cuda_integrate_point")
+        return out
+
+    def last_inwindow(self):
+        iw = ctypes.c_int64(0)
+        fb = ctypes.c_int64(0)
+        st = lib().teufel_cuda_last_inwindow(self.handle, ctypes.byref(iw), ctypes.byref(fb))
+        return int(iw.value), int(fb.value), st
+
+    def point_decisions(self, m, pos, t0, dt, nots):
+        n = int(self.n_points[m])
+        idx = np.zeros(n, dtype=np.int64)
+        flags = np.zeros(n, dtype=np.int32)
+        u = np.zeros(n)
+        pos = _c(pos).reshape(3)
+        check(lib().teufel_cuda_point_decisions(self.handle, m, _ptr(pos), t0, dt, nots,
+                                                _ptr(idx, _lp), _ptr(flags, _ip), _ptr(u)),
+              "teufel_cuda_point_decisions")
+        return idx, flags, u
+
+
+def deposit_injected(ts_list, f_list, t0, dt, nots, precision=PREC_FP64, trace=None):
+    """Device deposit of injected (arrival time, field) sequences."""
+    n_points = np.array([len(v) for v in ts_list], dtype=np.int32)
+    ts = _c(np.concatenate([np.asarray(v, dtype=np.float64) for v in ts_list]) if ts_list
+            else np.zeros(0))
+    f = _c(np.concatenate([np.asarray(v, dtype=np.float64).reshape(-1, 6) for v in f_list])
+           if f_list else np.zeros((0, 6)))
+    if trace is None:
+        trace = np.zeros((nots, 6))
+    st = lib().teufel_cuda_deposit_injected(len(ts_list), _ptr(n_points, _ip), _ptr(ts), _ptr(f),
+                                            t0, dt, nots, precision, _ptr(trace))
+    return trace, st
+
+
+def probe_peaks():
+    a = ctypes.c_double(0)
+    b = ctypes.c_double(0)
+    check(lib().teufel_cuda_probe_peaks(ctypes.byref(a), ctypes.byref(b)), "probe_peaks")
+    return a.value, b.value

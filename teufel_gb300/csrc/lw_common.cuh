@@ -1,0 +1,319 @@
+// lw_common.cuh -- device functions shared by the FP64 and the FP32-split
+// field-integration kernels.
+//
+// Everything that decides WHERE a trajectory step lands in a trace -- the
+// retarded time, the bin index round((ts - t0)/dt), and the window tests
+// against tmin/tmax -- is evaluated here with IEEE-rounded double intrinsics
+// (__dadd_rn, __dmul_rn, __ddiv_rn, __dsqrt_rn), which the compiler never
+// contracts into FMAs.  Given the same inputs this reproduces the reference's
+// values bit for bit:
+//   RetardedTime      src/particle.cpp:560-568   (t + |obs - x| / c)
+//   Vector::norm      src/vector.cpp:136-139     (sqrt(x*x + y*y + z*z))
+//   window, indices   src/particle.cpp:780-781, 805, 831, 833
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "lw_internal.h"
+#include "teufel_cuda.h"
+
+namespace teufel {
+
+// point flags
+constexpr int kLeTmin = 1;   // ts <= tmin  (the step starting here begins before the window)
+constexpr int kLtTmax = 2;   // ts <  tmax
+constexpr int kExact = 4;    // resolved by the exact FP64 evaluation
+
+struct Window {
+    double t0, dt, tmin, tmax;
+    int nt;
+};
+
+__device__ __forceinline__ Window make_window(double t0, double dt, int nt) {
+    Window w;
+    w.t0 = t0;
+    w.dt = dt;
+    w.nt = nt;
+    // tmin = t0 - dt*0.5; tmax = t0 + dt*((double)nots - 0.5)  (src/particle.cpp:780-781)
+    w.tmin = __dsub_rn(t0, __dmul_rn(dt, 0.5));
+    w.tmax = __dadd_rn(t0, __dmul_rn(dt, __dsub_rn((double)nt, 0.5)));
+    return w;
+}
+
+// The reference's retarded time of one trajectory point, bit-exact.
+__device__ __forceinline__ double exact_retarded_time(const double4_32a tx, const double3 obs) {
+    double rx = __dsub_rn(obs.x, tx.y);
+    double ry = __dsub_rn(obs.y, tx.z);
+    double rz = __dsub_rn(obs.z, tx.w);
+    double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+    double R = __dsqrt_rn(r2);
+    return __dadd_rn(tx.x, __ddiv_rn(R, kC));
+}
+
+// Bin index of an exact arrival time, clamped to [-2, nt+1].  The clamp keeps
+// every decision the deposit takes (indices below 0 only matter through the
+// tmin flag, indices above nt are capped to nt by the reference, :806, :834).
+__device__ __forceinline__ int exact_bin(double ts, const Window& w) {
+    double u = __ddiv_rn(__dsub_rn(ts, w.t0), w.dt);
+    u = fmax(-4.0, fmin(u, (double)w.nt + 4.0));
+    int k = (int)round(u);  // round(): half away from zero, as C's round()
+    return k < -2 ? -2 : (k > w.nt + 1 ? w.nt + 1 : k);
+}
+
+__device__ __forceinline__ int exact_flags(double ts, const Window& w) {
+    return (ts <= w.tmin ? kLeTmin : 0) | (ts < w.tmax ? kLtTmax : 0) | kExact;
+}
+
+// Fast arrival-time estimate for range searches only (FMA, approximate sqrt):
+// within a few ulp of the exact value; callers widen ranges by two steps.
+__device__ __forceinline__ double approx_retarded_time(const double4_32a tx, const double3 obs) {
+    double rx = obs.x - tx.y, ry = obs.y - tx.z, rz = obs.z - tx.w;
+    double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
+    return fma(sqrt(r2), 1.0 / kC, tx.x);
+}
+
+// In-window step range of one particle for one observer, found by bisection
+// on the (monotone) arrival time over steps [st_lo, st_hi).  Returns the
+// first and last step that may overlap [tmin, tmax]; an empty range has
+// first > last.  Widened by two steps on each side against rounding; the
+// per-step exact decisions then select exactly the reference's steps.
+__device__ __forceinline__ void inwindow_steps(const double4_32a* tx, int st_lo, int st_hi,
+                                               const double3 obs, const Window& w, int* first,
+                                               int* last) {
+    // first point with ts > tmin in [st_lo, st_hi]
+    int lo = st_lo, hi = st_hi + 1;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (approx_retarded_time(tx[mid], obs) > w.tmin) hi = mid; else lo = mid + 1;
+    }
+    int i_first = lo;
+    // last point with ts < tmax in [st_lo, st_hi]
+    lo = st_lo - 1;
+    hi = st_hi;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (approx_retarded_time(tx[mid], obs) < w.tmax) lo = mid; else hi = mid - 1;
+    }
+    int j_last = lo;
+    int f = i_first - 1 - 2;
+    int l = j_last + 2;
+    *first = f < st_lo ? st_lo : f;
+    *last = l > st_hi - 1 ? st_hi - 1 : l;
+}
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies for the deposit: the FP64 path uses IEEE-rounded
+// operations in the reference's order, the FP32 path plain float operations.
+// ---------------------------------------------------------------------------
+struct Ops64 {
+    typedef double T;
+    __device__ static T add(T a, T b) { return __dadd_rn(a, b); }
+    __device__ static T sub(T a, T b) { return __dsub_rn(a, b); }
+    __device__ static T mul(T a, T b) { return __dmul_rn(a, b); }
+    __device__ static T div(T a, T b) { return __ddiv_rn(a, b); }
+};
+struct Ops32 {
+    typedef float T;
+    __device__ static T add(T a, T b) { return a + b; }
+    __device__ static T sub(T a, T b) { return a - b; }
+    __device__ static T mul(T a, T b) { return a * b; }
+    __device__ static T div(T a, T b) { return __fdividef(a, b); }
+};
+
+// Time coordinates of the bins.  Geo64 works in seconds exactly as the
+// reference (t_center = t0 + idx*dt etc., src/particle.cpp:812, 816, 845,
+// 851, 856); Geo32 works in bin units relative to an integer base B.
+struct Geo64 {
+    double t0, dt;
+    __device__ double center(int k) const { return __dadd_rn(t0, __dmul_rn((double)k, dt)); }
+    __device__ double start(int k) const {
+        return __dadd_rn(t0, __dmul_rn(__dsub_rn((double)k, 0.5), dt));
+    }
+    __device__ double end(int k) const {
+        return __dadd_rn(t0, __dmul_rn(__dadd_rn((double)k, 0.5), dt));
+    }
+    __device__ double per_dt(double x) const { return __ddiv_rn(x, dt); }
+};
+struct Geo32 {
+    long long B;
+    __device__ float center(int k) const { return (float)((long long)k - B); }
+    __device__ float start(int k) const { return (float)((long long)k - B) - 0.5f; }
+    __device__ float end(int k) const { return (float)((long long)k - B) + 0.5f; }
+    __device__ float per_dt(float x) const { return x; }
+};
+
+// One step of ChargedParticle::integrateFieldTrace (src/particle.cpp:786-865):
+// the linear interpolant of the field over [ts1, ts2] is averaged over every
+// bin it overlaps.  Decisions (window, case, indices) come from the point
+// flags and bin indices; weights come from the coordinates u1, u2.
+// Sink::add(k, f[6]) receives the bin contributions in increasing k.
+template <class Ops, class Geo, class Sink>
+__device__ __forceinline__ bool deposit_step(typename Ops::T u1, typename Ops::T u2, int idx1,
+                                             int flags1, int idx2, int flags2,
+                                             const typename Ops::T* f1,
+                                             const typename Ops::T* f2, const Geo& geo, int nt,
+                                             Sink& sink) {
+    typedef typename Ops::T T;
+    // (ts2 > tmin) && (ts1 < tmax)
+    if ((flags2 & kLeTmin) || !(flags1 & kLtTmax)) return false;
+    T dts = Ops::sub(u2, u1);
+    T field[6];
+    if (idx2 > nt) idx2 = nt;
+    if (flags1 & kLeTmin) {
+        // the step starts before the window: bins 0 .. idx2-1 fully covered
+        for (int k = 0; k < idx2; k++) {
+            T tc = geo.center(k);
+            T w1 = Ops::div(Ops::sub(u2, tc), dts), w2 = Ops::div(Ops::sub(tc, u1), dts);
+#pragma unroll
+            for (int c = 0; c < 6; c++) field[c] = Ops::add(Ops::mul(f1[c], w1), Ops::mul(f2[c], w2));
+            sink.add(k, field);
+        }
+        if (idx2 < nt) {
+            T ts = geo.start(idx2);
+            T w1 = Ops::div(Ops::sub(u2, ts), dts), w2 = Ops::div(Ops::sub(ts, u1), dts);
+            T wb = geo.per_dt(Ops::sub(u2, ts));
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                T fs = Ops::add(Ops::mul(f1[c], w1), Ops::mul(f2[c], w2));
+                field[c] = Ops::mul(Ops::mul(Ops::add(fs, f2[c]), (T)0.5), wb);
+            }
+            sink.add(idx2, field);
+        }
+    } else {
+        if (idx1 == idx2) {
+            // the step lies within one bin
+            T wb = geo.per_dt(dts);
+#pragma unroll
+            for (int c = 0; c < 6; c++)
+                field[c] = Ops::mul(Ops::mul(Ops::add(f1[c], f2[c]), (T)0.5), wb);
+            sink.add(idx1, field);
+        } else {
+            // first partial bin
+            T te = geo.end(idx1);
+            T w1 = Ops::div(Ops::sub(u2, te), dts), w2 = Ops::div(Ops::sub(te, u1), dts);
+            T wb = geo.per_dt(Ops::sub(te, u1));
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                T fe = Ops::add(Ops::mul(f1[c], w1), Ops::mul(f2[c], w2));
+                field[c] = Ops::mul(Ops::mul(Ops::add(f1[c], fe), (T)0.5), wb);
+            }
+            sink.add(idx1, field);
+            // fully covered bins
+            for (int k = idx1 + 1; k < idx2; k++) {
+                T tc = geo.center(k);
+                T v1 = Ops::div(Ops::sub(u2, tc), dts), v2 = Ops::div(Ops::sub(tc, u1), dts);
+#pragma unroll
+                for (int c = 0; c < 6; c++)
+                    field[c] = Ops::add(Ops::mul(f1[c], v1), Ops::mul(f2[c], v2));
+                sink.add(k, field);
+            }
+            // last partial bin
+            if (idx2 < nt) {
+                T ts = geo.start(idx2);
+                T x1 = Ops::div(Ops::sub(u2, ts), dts), x2 = Ops::div(Ops::sub(ts, u1), dts);
+                T wl = geo.per_dt(Ops::sub(u2, ts));
+#pragma unroll
+                for (int c = 0; c < 6; c++) {
+                    T fs = Ops::add(Ops::mul(f1[c], x1), Ops::mul(f2[c], x2));
+                    field[c] = Ops::mul(Ops::mul(Ops::add(fs, f2[c]), (T)0.5), wl);
+                }
+                sink.add(idx2, field);
+            }
+        }
+    }
+    return true;
+}
+
+// Read-modify-write of one bin (6 components, 8- resp. 16-byte aligned).
+__device__ __forceinline__ void add_row(float* row, const float* a) {
+    float2* p = reinterpret_cast<float2*>(row);
+    float2 v0 = p[0], v1 = p[1], v2 = p[2];
+    v0.x += a[0];
+    v0.y += a[1];
+    v1.x += a[2];
+    v1.y += a[3];
+    v2.x += a[4];
+    v2.y += a[5];
+    p[0] = v0;
+    p[1] = v1;
+    p[2] = v2;
+}
+__device__ __forceinline__ void add_row(double* row, const double* a) {
+    double2* p = reinterpret_cast<double2*>(row);
+    double2 v0 = p[0], v1 = p[1], v2 = p[2];
+    v0.x = __dadd_rn(v0.x, a[0]);
+    v0.y = __dadd_rn(v0.y, a[1]);
+    v1.x = __dadd_rn(v1.x, a[2]);
+    v1.y = __dadd_rn(v1.y, a[3]);
+    v2.x = __dadd_rn(v2.x, a[4]);
+    v2.y = __dadd_rn(v2.y, a[5]);
+    p[0] = v0;
+    p[1] = v1;
+    p[2] = v2;
+}
+
+// Accumulates the contributions of consecutive deposits into the open bin in
+// registers and adds a finished bin into the pixel's partial trace.  Bins
+// outside [0, nt) are the reference's range error: recorded and skipped.
+template <class T, int STRIDE>
+struct BinSink {
+    T a[6];
+    int open;
+    int nt;
+    T* row;  // this pixel's partial trace, [nt][STRIDE]
+    unsigned int err;
+    __device__ void init(T* r, int n) {
+        row = r;
+        nt = n;
+        open = -1;
+        err = 0;
+    }
+    __device__ __forceinline__ void add(int k, const T* f) {
+        if (k < 0 || k >= nt) {
+            err |= 1u << TEUFEL_ERR_RANGE;
+            return;
+        }
+        if (k == open) {
+#pragma unroll
+            for (int c = 0; c < 6; c++) a[c] += f[c];
+        } else {
+            flush();
+            open = k;
+#pragma unroll
+            for (int c = 0; c < 6; c++) a[c] = f[c];
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        if (open < 0) return;
+        add_row(row + (int64_t)open * STRIDE, a);
+        open = -1;
+    }
+};
+
+// Scale of the Lienard-Wiechert field of one particle:
+// Charge*ElementaryCharge/(4.0*Pi*EpsNull), evaluated as src/particle.cpp:587.
+__device__ __forceinline__ double field_scale(double charge) {
+    return __ddiv_rn(__dmul_rn(charge, kE), __dmul_rn(__dmul_rn(4.0, kPi), kEps0));
+}
+
+__device__ __forceinline__ int warp_min(int v) { return __reduce_min_sync(0xffffffffu, v); }
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_max(int v) { return __reduce_max_sync(0xffffffffu, v); }
+
+// First particle whose segment range ends after global segment g.
+__device__ __forceinline__ int particle_of_segment(const int64_t* seg_offsets, int n, int64_t g) {
+    int lo = 0, hi = n;  // seg_offsets[n] = total
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (seg_offsets[mid + 1] > g) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+}  // namespace teufel

@@ -1,0 +1,79 @@
+// lw_internal.h -- structures shared by the host side of the C-ABI and the
+// kernels of the Lienard-Wiechert field integration.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace teufel {
+
+// Physical constants, src/global.h:36-44 of the reference.
+constexpr double kC = 2.99792458e8;
+constexpr double kE = 1.6021766208e-19;
+constexpr double kPi = 3.1415926535897932384626433832795029;
+constexpr double kEps0 = 8.854187817e-12;
+
+// Trajectory points are grouped into segments of kSegLen steps.  Segment k of
+// a particle owns steps [k*kSegLen, (k+1)*kSegLen) and its first point is the
+// FP64 anchor from which the FP32 path measures positions and arrival times.
+constexpr int kSegShift = 6;
+constexpr int kSegLen = 1 << kSegShift;
+
+// Device view of a resident trajectory set.
+struct DevTraj {
+    int n_particles;
+    int64_t n_points;           // total points
+    int64_t n_segments;         // total segments
+    const int64_t* offsets;     // [n+1] first point of each particle
+    const int64_t* seg_offsets; // [n+1] first segment of each particle
+    const double* charge;       // [n] units of e
+    const double4_32a* vhat;        // [n] frame direction of each particle (mean velocity), w = monotone flag
+    const double4_32a* tx;          // [Npts] t, x, y, z                 (FP64, as uploaded)
+    const double4_32a* pp;          // [Npts] beta*gamma, w unused        (FP64)
+    const double4_32a* aa;          // [Npts] d(beta*gamma)/dt, w unused  (FP64)
+    const float4* q0;           // [Npts] e = x - x_anchor (xyz), dtau = (t - t_a) - vhat.e/c
+    const float4* q1;           // [Npts] beta-hat (xyz), eps = 1 - |beta|
+    const float4* q2;           // [Npts] A/gamma*scale/c (xyz), scale/gamma^2
+    const float4* segb;         // [Nseg] max|dtau|, max|vhat.e|, max|e_perp|, max|e|
+};
+
+// One observer handed to a kernel launch.
+struct DevScreen {
+    const double* pix_pos;  // [Np][3]
+    const double* pix_t0;   // [Np]
+    int np;
+    int nt;
+    double dt;
+};
+
+// Work split: slot s integrates global segments [slot_seg[s], slot_seg[s+1]).
+struct DevWork {
+    int n_slots;
+    const int64_t* slot_seg;  // [n_slots+1]
+    void* scratch;            // per-slot partial traces
+    int64_t slot_stride;      // elements between slots
+    unsigned int* status;     // bit mask of TEUFEL_ERR_* seen on the device
+    unsigned long long* counters;  // [0] in-window triples, [1] exact-fallback points
+};
+
+}  // namespace teufel
+
+// Kernel launchers (defined in the .cu files)
+namespace teufel {
+cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
+                        cudaStream_t s);
+cudaError_t launch_fp64(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
+                        cudaStream_t s);
+cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* out,
+                               cudaStream_t s);
+cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* out,
+                               cudaStream_t s);
+cudaError_t launch_point_decisions(const DevTraj& tr, int m, double3 pos, double t0, double dt,
+                                   int nt, int64_t* idx, int* flags, double* u_est,
+                                   unsigned int* status, cudaStream_t s);
+cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const double* ts,
+                                    const double* f, double t0, double dt, int nt, int precision,
+                                    double* trace, unsigned int* status, cudaStream_t s);
+cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s);
+int probe_peaks(double* fp32_tflops, double* fp64_tflops);
+}  // namespace teufel

@@ -1,0 +1,206 @@
+// lw_support.cu -- the FP64 reduction of the per-slot partial traces, the
+// device deposit on injected arrival times (for the known-answer test), and
+// the FP32/FP64 throughput probes used as roofline denominators.
+#include <cuda_runtime.h>
+
+#include "lw_common.cuh"
+
+namespace teufel {
+
+// out[p][k][c] += sum over slots (in slot order, FP64) of the partial
+// traces; the partial slots are cleared for the next call.  The FP32 path
+// stores c*B, so the B components are divided by c here.
+__global__ void reduce_fp32_kernel(DevWork w, int64_t n_bins, double* out) {
+    const float* scr = static_cast<const float*>(w.scratch);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < w.n_slots; s++) {
+            float2* p = (float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
+            float2 a = p[0], b = p[1], c = p[2];
+            acc[0] += (double)a.x;
+            acc[1] += (double)a.y;
+            acc[2] += (double)b.x;
+            acc[3] += (double)b.y;
+            acc[4] += (double)c.x;
+            acc[5] += (double)c.y;
+            float2 z = make_float2(0.0f, 0.0f);
+            p[0] = z;
+            p[1] = z;
+            p[2] = z;
+        }
+        double* o = out + e * 6;
+        o[0] += acc[0];
+        o[1] += acc[1];
+        o[2] += acc[2];
+        o[3] += acc[3] / kC;
+        o[4] += acc[4] / kC;
+        o[5] += acc[5] / kC;
+    }
+}
+
+__global__ void reduce_fp64_kernel(DevWork w, int64_t n_bins, double* out) {
+    const double* scr = static_cast<const double*>(w.scratch);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < w.n_slots; s++) {
+            double2* p = (double2*)(scr + (int64_t)s * w.slot_stride + e * 6);
+            double2 a = p[0], b = p[1], c = p[2];
+            acc[0] += a.x;
+            acc[1] += a.y;
+            acc[2] += b.x;
+            acc[3] += b.y;
+            acc[4] += c.x;
+            acc[5] += c.y;
+            double2 z = make_double2(0.0, 0.0);
+            p[0] = z;
+            p[1] = z;
+            p[2] = z;
+        }
+        double* o = out + e * 6;
+#pragma unroll
+        for (int c = 0; c < 6; c++) o[c] += acc[c];
+    }
+}
+
+static unsigned reduce_blocks(int64_t n_bins) {
+    int64_t b = (n_bins + 255) / 256;
+    return (unsigned)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+
+cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* out,
+                               cudaStream_t s) {
+    int64_t n = (int64_t)sc.np * sc.nt;
+    if (n == 0) return cudaSuccess;
+    reduce_fp32_kernel<<<reduce_blocks(n), 256, 0, s>>>(w, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* out,
+                               cudaStream_t s) {
+    int64_t n = (int64_t)sc.np * sc.nt;
+    if (n == 0) return cudaSuccess;
+    reduce_fp64_kernel<<<reduce_blocks(n), 256, 0, s>>>(w, n, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Deposit of injected (ts, field) sequences: the reference's known-answer
+// test replaces RetardedTime/RetardedField by fixed values
+// (tests/teufel.integrate_field.cpp:51-78); this runs the device deposit on
+// such values.  One thread, particles in order.
+// ---------------------------------------------------------------------------
+__global__ void deposit_injected_kernel(int n_part, const int64_t* offs, const double* ts,
+                                        const double* f, double t0, double dt, int nt,
+                                        int precision, double* trace, float* trace32,
+                                        unsigned int* status) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    Window w = make_window(t0, dt, nt);
+    unsigned int err = 0;
+    if (precision == TEUFEL_PREC_FP64) {
+        BinSink<double, 6> sink;
+        sink.init(trace, nt);
+        Geo64 geo{t0, dt};
+        for (int m = 0; m < n_part; m++) {
+            int64_t o = offs[m], n = offs[m + 1] - o;
+            for (int64_t s = 0; s + 1 < n; s++) {
+                double a = ts[o + s], b = ts[o + s + 1];
+                deposit_step<Ops64>(a, b, exact_bin(a, w), exact_flags(a, w), exact_bin(b, w),
+                                    exact_flags(b, w), f + 6 * (o + s), f + 6 * (o + s + 1), geo,
+                                    nt, sink);
+            }
+        }
+        sink.flush();
+        err = sink.err;
+    } else {
+        BinSink<float, 6> sink;
+        sink.init(trace32, nt);
+        Geo32 geo{0};
+        for (int m = 0; m < n_part; m++) {
+            int64_t o = offs[m], n = offs[m + 1] - o;
+            for (int64_t s = 0; s + 1 < n; s++) {
+                double a = ts[o + s], b = ts[o + s + 1];
+                float f1[6], f2[6];
+                for (int c = 0; c < 6; c++) {
+                    f1[c] = (float)f[6 * (o + s) + c];
+                    f2[c] = (float)f[6 * (o + s + 1) + c];
+                }
+                deposit_step<Ops32>((float)((a - t0) / dt), (float)((b - t0) / dt),
+                                    exact_bin(a, w), exact_flags(a, w), exact_bin(b, w),
+                                    exact_flags(b, w), f1, f2, geo, nt, sink);
+            }
+        }
+        sink.flush();
+        err = sink.err;
+        for (int k = 0; k < 6 * nt; k++) trace[k] += (double)trace32[k];
+    }
+    if (err) atomicOr(status, err);
+}
+
+cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const double* ts,
+                                    const double* f, double t0, double dt, int nt, int precision,
+                                    double* trace, unsigned int* status, cudaStream_t s) {
+    float* t32 = nullptr;
+    cudaError_t e = cudaMallocAsync(&t32, sizeof(float) * 6 * (size_t)(nt > 0 ? nt : 1), s);
+    if (e != cudaSuccess) return e;
+    cudaMemsetAsync(t32, 0, sizeof(float) * 6 * (size_t)(nt > 0 ? nt : 1), s);
+    deposit_injected_kernel<<<1, 32, 0, s>>>(n_part, offs, ts, f, t0, dt, nt, precision, trace,
+                                             t32, status);
+    e = cudaGetLastError();
+    cudaFreeAsync(t32, s);
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// Throughput probes
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void fma_probe_kernel(T* out, int iters, T b, T c) {
+    T x0 = (T)threadIdx.x, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+    T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+    for (int i = 0; i < iters; i++) {
+        x0 = fma(x0, b, c);
+        x1 = fma(x1, b, c);
+        x2 = fma(x2, b, c);
+        x3 = fma(x3, b, c);
+        x4 = fma(x4, b, c);
+        x5 = fma(x5, b, c);
+        x6 = fma(x6, b, c);
+        x7 = fma(x7, b, c);
+    }
+    T s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == (T)-1.2345) out[0] = s;  // keeps the chains live
+}
+
+template <class T>
+static double time_probe(int iters, int blocks, int threads) {
+    T* out = nullptr;
+    if (cudaMalloc(&out, sizeof(T)) != cudaSuccess) return 0.0;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    fma_probe_kernel<T><<<blocks, threads>>>(out, iters / 10, (T)0.999, (T)0.001);  // warm-up
+    cudaEventRecord(a);
+    fma_probe_kernel<T><<<blocks, threads>>>(out, iters, (T)0.999, (T)0.001);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    double flops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads;
+    return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+}
+
+int probe_peaks(double* fp32_tflops, double* fp64_tflops) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (fp32_tflops) *fp32_tflops = time_probe<float>(1 << 16, sms * 8, 256);
+    if (fp64_tflops) *fp64_tflops = time_probe<double>(1 << 11, sms * 8, 256);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+}  // namespace teufel

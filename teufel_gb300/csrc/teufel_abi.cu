@@ -1,0 +1,478 @@
+// teufel_abi.cu -- host side of the C-ABI declared in include/teufel_cuda.h.
+//
+// Owns the device-resident trajectory store, the per-slot partial traces and
+// the staging of observer buffers; launches the field-integration kernels
+// and the FP64 reduction.  Every entry point returns a status code and
+// never throws across the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "lw_internal.h"
+#include "teufel_cuda.h"
+
+using namespace teufel;
+
+struct teufel_traj_set {
+    int device = 0;
+    DevTraj dev{};
+    std::vector<void*> owned;  // trajectory arrays
+    // grow-only work buffers
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int64_t* slot_seg = nullptr;
+    int slot_cap = 0;
+    double* d_pix = nullptr;
+    size_t pix_cap = 0;  // doubles
+    double* d_out = nullptr;
+    size_t out_cap = 0;  // doubles
+    unsigned int* d_status = nullptr;
+    unsigned long long* d_counters = nullptr;
+    unsigned long long last_counters[2] = {0, 0};
+    std::vector<int64_t> h_seg_offsets;
+};
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int64_t kMaxParticlesPerSlotFp32 = 2048;
+
+#define TRY_CUDA(call)                              \
+    do {                                            \
+        cudaError_t e_ = (call);                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_); \
+    } while (0)
+
+int cuda_fail(cudaError_t e) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return TEUFEL_ERR_NOMEM;
+    }
+    cudaGetLastError();
+    return TEUFEL_ERR_CUDA;
+}
+
+int check_device() {
+    int dev = 0, n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return TEUFEL_ERR_NODEVICE;
+    }
+    if (cudaGetDevice(&dev) != cudaSuccess) return TEUFEL_ERR_NODEVICE;
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3) return TEUFEL_ERR_NODEVICE;
+    return TEUFEL_OK;
+}
+
+template <class T>
+int dev_alloc(teufel_traj_set* h, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e != cudaSuccess) return cuda_fail(e);
+    h->owned.push_back(*p);
+    return TEUFEL_OK;
+}
+
+int grow(void** p, size_t* cap, size_t bytes, bool zero) {
+    if (*cap >= bytes && *p) return TEUFEL_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (zero) {
+        e = cudaMemset(*p, 0, bytes ? bytes : 16);
+        if (e != cudaSuccess) return cuda_fail(e);
+    }
+    *cap = bytes;
+    return TEUFEL_OK;
+}
+
+__global__ void pack_points_kernel(int64_t n, const double* t, const double* x, const double* bg,
+                                   const double* a, double4_32a* tx, double4_32a* pp, double4_32a* aa,
+                                   unsigned int* status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v[10] = {t[i],          x[3 * i],      x[3 * i + 1],  x[3 * i + 2], bg[3 * i],
+                    bg[3 * i + 1], bg[3 * i + 2], a[3 * i],      a[3 * i + 1], a[3 * i + 2]};
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 10; k++) ok = ok && isfinite(v[k]);
+    if (!ok) atomicOr(status, 1u << TEUFEL_ERR_ARG);
+    tx[i] = make_double4_32a(v[0], v[1], v[2], v[3]);
+    pp[i] = make_double4_32a(v[4], v[5], v[6], 0.0);
+    aa[i] = make_double4_32a(v[7], v[8], v[9], 0.0);
+}
+
+int status_from_mask(unsigned int mask) {
+    if (mask & (1u << TEUFEL_ERR_ARG)) return TEUFEL_ERR_ARG;
+    if (mask & (1u << TEUFEL_ERR_RANGE)) return TEUFEL_ERR_RANGE;
+    if (mask) return TEUFEL_ERR_CUDA;
+    return TEUFEL_OK;
+}
+
+bool finite_array(const double* p, int64_t n) {
+    for (int64_t i = 0; i < n; i++)
+        if (!std::isfinite(p[i])) return false;
+    return true;
+}
+
+// Device part of an integration: partial traces per slot, then the FP64
+// reduction into out (device pointers).  Enqueued on s.
+int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
+               int np, double* d_out, const teufel_options& opt, cudaStream_t s) {
+    const bool fp64 = opt.precision == TEUFEL_PREC_FP64;
+    const int64_t G = h->dev.n_segments;
+    const size_t elem = fp64 ? sizeof(double) : sizeof(float);
+    const size_t slot_bytes = (size_t)np * (size_t)nt * 6 * elem;
+    const int pix_blocks = (np + kThreads - 1) / kThreads;
+    int64_t target = opt.n_slots > 0 ? opt.n_slots
+                                     : (152LL * 512 * 4 + (int64_t)pix_blocks * kThreads - 1) /
+                                           ((int64_t)pix_blocks * kThreads);
+    int64_t slots_total = std::max<int64_t>(target, 1);
+    if (!fp64 && opt.n_slots <= 0)
+        slots_total = std::max<int64_t>(
+            slots_total, (h->dev.n_particles + kMaxParticlesPerSlotFp32 - 1) / kMaxParticlesPerSlotFp32);
+    slots_total = std::min<int64_t>(slots_total, std::max<int64_t>(G, 1));
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    size_t budget = std::min<size_t>((size_t)48 << 30, (size_t)(0.4 * (double)(free_b + h->scratch_bytes)));
+    int64_t per_pass = slot_bytes ? (int64_t)(budget / slot_bytes) : slots_total;
+    per_pass = std::max<int64_t>(1, std::min<int64_t>(per_pass, slots_total));
+    int rc = grow(&h->scratch, &h->scratch_bytes, slot_bytes * (size_t)per_pass, true);
+    if (rc) return rc;
+    std::vector<int64_t> bounds(slots_total + 1);
+    for (int64_t k = 0; k <= slots_total; k++) bounds[k] = G * k / slots_total;
+    if (h->slot_cap < slots_total + 1) {
+        if (h->slot_seg) cudaFree(h->slot_seg);
+        h->slot_seg = nullptr;
+        h->slot_cap = 0;
+        TRY_CUDA(cudaMalloc(&h->slot_seg, sizeof(int64_t) * (slots_total + 1)));
+        h->slot_cap = (int)(slots_total + 1);
+    }
+    TRY_CUDA(cudaMemcpyAsync(h->slot_seg, bounds.data(), sizeof(int64_t) * (slots_total + 1),
+                             cudaMemcpyHostToDevice, s));
+    TRY_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), s));
+    TRY_CUDA(cudaMemsetAsync(h->d_counters, 0, 2 * sizeof(unsigned long long), s));
+    DevScreen sc{d_pos, d_t0, np, nt, dt};
+    for (int64_t p0 = 0; p0 < slots_total; p0 += per_pass) {
+        DevWork w;
+        w.n_slots = (int)std::min<int64_t>(per_pass, slots_total - p0);
+        w.slot_seg = h->slot_seg + p0;
+        w.scratch = h->scratch;
+        w.slot_stride = (int64_t)np * nt * 6;
+        w.status = h->d_status;
+        w.counters = h->d_counters;
+        cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
+                             : launch_fp32(h->dev, sc, w, kThreads, s);
+        if (e != cudaSuccess) return cuda_fail(e);
+        e = fp64 ? launch_reduce_fp64(w, sc, d_out, s) : launch_reduce_fp32(w, sc, d_out, s);
+        if (e != cudaSuccess) return cuda_fail(e);
+    }
+    return TEUFEL_OK;
+}
+
+int finish(teufel_traj_set* h, cudaStream_t s) {
+    unsigned int mask = 0;
+    TRY_CUDA(cudaMemcpyAsync(&mask, h->d_status, sizeof(mask), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaMemcpyAsync(h->last_counters, h->d_counters, sizeof(h->last_counters),
+                             cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaStreamSynchronize(s));
+    return status_from_mask(mask);
+}
+
+bool valid_screen_args(const teufel_traj_set* traj, const double* pos, const double* t0,
+                       double dt, int nt, int np, const double* out) {
+    if (!traj || nt < 0 || np < 0) return false;
+    if (np > 0 && nt > 0 && (!pos || !t0 || !out)) return false;
+    if (!std::isfinite(dt)) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void teufel_cuda_default_options(teufel_options* opt) {
+    if (!opt) return;
+    opt->precision = TEUFEL_PREC_FP32_SPLIT;
+    opt->device_pointers = 0;
+    opt->n_slots = 0;
+    opt->threads_per_block = 0;
+}
+
+const char* teufel_cuda_status_string(int status) {
+    switch (status) {
+        case TEUFEL_OK: return "ok";
+        case TEUFEL_ERR_ARG: return "bad argument";
+        case TEUFEL_ERR_NOMEM: return "out of memory";
+        case TEUFEL_ERR_CUDA: return "CUDA error";
+        case TEUFEL_ERR_RANGE: return "FieldTrace::add - index out of range.";
+        case TEUFEL_ERR_NODEVICE: return "no sm_103 CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* charge_e,
+                            const double* t, const double* x, const double* bg, const double* a,
+                            teufel_traj_set** out) {
+    if (!out) return TEUFEL_ERR_ARG;
+    *out = nullptr;
+    if (n_particles < 0 || (n_particles > 0 && (!n_points || !charge_e))) return TEUFEL_ERR_ARG;
+    int rc = check_device();
+    if (rc) return rc;
+    std::vector<int64_t> offs(n_particles + 1, 0), segs(n_particles + 1, 0);
+    for (int m = 0; m < n_particles; m++) {
+        if (n_points[m] < 0) return TEUFEL_ERR_ARG;
+        offs[m + 1] = offs[m] + n_points[m];
+        int64_t nseg = n_points[m] >= 1 ? ((int64_t)(n_points[m] - 1) >> kSegShift) + 1 : 0;
+        segs[m + 1] = segs[m] + nseg;
+    }
+    const int64_t N = offs[n_particles];
+    if (N > 0 && (!t || !x || !bg || !a)) return TEUFEL_ERR_ARG;
+    if (!finite_array(charge_e, n_particles)) return TEUFEL_ERR_ARG;
+    teufel_traj_set* h = new (std::nothrow) teufel_traj_set();
+    if (!h) return TEUFEL_ERR_NOMEM;
+    h->h_seg_offsets = segs;
+    cudaGetDevice(&h->device);
+    auto fail = [&](int code) {
+        teufel_cuda_traj_free(h);
+        return code;
+    };
+    DevTraj& d = h->dev;
+    d.n_particles = n_particles;
+    d.n_points = N;
+    d.n_segments = segs[n_particles];
+    int64_t *p_off, *p_seg;
+    double* p_charge;
+    double4_32a *p_vhat, *p_tx, *p_pp, *p_aa;
+    float4 *p_q0, *p_q1, *p_q2, *p_segb;
+    if ((rc = dev_alloc(h, &p_off, n_particles + 1)) || (rc = dev_alloc(h, &p_seg, n_particles + 1)) ||
+        (rc = dev_alloc(h, &p_charge, n_particles)) || (rc = dev_alloc(h, &p_vhat, n_particles)) ||
+        (rc = dev_alloc(h, &p_tx, N)) || (rc = dev_alloc(h, &p_pp, N)) ||
+        (rc = dev_alloc(h, &p_aa, N)) || (rc = dev_alloc(h, &p_q0, N)) ||
+        (rc = dev_alloc(h, &p_q1, N)) || (rc = dev_alloc(h, &p_q2, N)) ||
+        (rc = dev_alloc(h, &p_segb, d.n_segments)))
+        return fail(rc);
+    if (cudaMalloc(&h->d_status, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc(&h->d_counters, 2 * sizeof(unsigned long long)) != cudaSuccess)
+        return fail(cuda_fail(cudaErrorMemoryAllocation));
+    d.offsets = p_off;
+    d.seg_offsets = p_seg;
+    d.charge = p_charge;
+    d.vhat = p_vhat;
+    d.tx = p_tx;
+    d.pp = p_pp;
+    d.aa = p_aa;
+    d.q0 = p_q0;
+    d.q1 = p_q1;
+    d.q2 = p_q2;
+    d.segb = p_segb;
+    cudaStream_t s = 0;
+    if (cudaMemcpy(p_off, offs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(p_seg, segs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
+        (n_particles > 0 &&
+         cudaMemcpy(p_charge, charge_e, sizeof(double) * n_particles, cudaMemcpyHostToDevice)) ||
+        cudaMemset(h->d_status, 0, sizeof(unsigned int)))
+        return fail(cuda_fail(cudaGetLastError()));
+    if (N > 0) {
+        // raw arrays to the device, then packed there
+        double* raw = nullptr;
+        if (cudaMalloc(&raw, sizeof(double) * 10 * (size_t)N) != cudaSuccess)
+            return fail(cuda_fail(cudaErrorMemoryAllocation));
+        double *rt = raw, *rx = raw + N, *rb = raw + 4 * N, *ra = raw + 7 * N;
+        cudaError_t e = cudaMemcpyAsync(rt, t, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(rx, x, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(rb, bg, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(ra, a, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+        if (!e) {
+            pack_points_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(
+                N, rt, rx, rb, ra, p_tx, p_pp, p_aa, h->d_status);
+            e = cudaGetLastError();
+        }
+        if (!e) e = launch_prep_points(d, s);
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        cudaFree(raw);
+        if (e || e2) return fail(cuda_fail(e ? e : e2));
+    } else if (n_particles > 0) {
+        if (launch_prep_points(d, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError()));
+    }
+    unsigned int mask = 0;
+    if (cudaMemcpy(&mask, h->d_status, sizeof(mask), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError()));
+    if (mask) return fail(status_from_mask(mask));
+    *out = h;
+    return TEUFEL_OK;
+}
+
+int teufel_cuda_traj_free(teufel_traj_set* traj) {
+    if (!traj) return TEUFEL_OK;
+    for (void* p : traj->owned) cudaFree(p);
+    if (traj->scratch) cudaFree(traj->scratch);
+    if (traj->slot_seg) cudaFree(traj->slot_seg);
+    if (traj->d_pix) cudaFree(traj->d_pix);
+    if (traj->d_out) cudaFree(traj->d_out);
+    if (traj->d_status) cudaFree(traj->d_status);
+    if (traj->d_counters) cudaFree(traj->d_counters);
+    delete traj;
+    return TEUFEL_OK;
+}
+
+int64_t teufel_cuda_traj_points(const teufel_traj_set* traj) {
+    return traj ? traj->dev.n_points : 0;
+}
+
+int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double* pix_pos,
+                                    const double* pix_t0, double dt, int Nt, int Np, double* out,
+                                    const teufel_options* opt_in, teufel_stream_t stream) {
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj_c);
+    if (!valid_screen_args(h, pix_pos, pix_t0, dt, Nt, Np, out)) return TEUFEL_ERR_ARG;
+    teufel_options opt;
+    teufel_cuda_default_options(&opt);
+    if (opt_in) opt = *opt_in;
+    if (opt.precision != TEUFEL_PREC_FP32_SPLIT && opt.precision != TEUFEL_PREC_FP64)
+        return TEUFEL_ERR_ARG;
+    h->last_counters[0] = h->last_counters[1] = 0;
+    // the reference returns early for traces shorter than 2 samples and for
+    // trajectories shorter than 2 points (src/particle.cpp:778, 783)
+    if (Nt < 2 || Np == 0 || h->dev.n_particles == 0 || h->dev.n_segments == 0) return TEUFEL_OK;
+    if (!(dt > 0.0) && !(dt < 0.0)) return TEUFEL_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc;
+    if (opt.device_pointers) {
+        return run_device(h, pix_pos, pix_t0, dt, Nt, Np, out, opt, s);
+    }
+    if (!finite_array(pix_pos, 3 * (int64_t)Np) || !finite_array(pix_t0, Np)) return TEUFEL_ERR_ARG;
+    const size_t nout = (size_t)Np * (size_t)Nt * 6;
+    if ((rc = grow((void**)&h->d_pix, &h->pix_cap, sizeof(double) * 4 * (size_t)Np, false))) return rc;
+    if ((rc = grow((void**)&h->d_out, &h->out_cap, sizeof(double) * nout, false))) return rc;
+    double* d_pos = h->d_pix;
+    double* d_t0 = h->d_pix + 3 * (size_t)Np;
+    TRY_CUDA(cudaMemcpyAsync(d_pos, pix_pos, sizeof(double) * 3 * Np, cudaMemcpyHostToDevice, s));
+    TRY_CUDA(cudaMemcpyAsync(d_t0, pix_t0, sizeof(double) * Np, cudaMemcpyHostToDevice, s));
+    TRY_CUDA(cudaMemcpyAsync(h->d_out, out, sizeof(double) * nout, cudaMemcpyHostToDevice, s));
+    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s);
+    if (rc) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    TRY_CUDA(cudaMemcpyAsync(out, h->d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+    return finish(h, s);
+}
+
+int teufel_cuda_integrate_screen(const teufel_traj_set* traj, const double* pix_pos,
+                                 const double* pix_t0, double dt, int Nt, int Np, double* out,
+                                 teufel_stream_t s) {
+    return teufel_cuda_integrate_screen_ex(traj, pix_pos, pix_t0, dt, Nt, Np, out, nullptr, s);
+}
+
+int teufel_cuda_integrate_point(const teufel_traj_set* traj, const double* pos, double t0,
+                                double dt, int Nt, double* out, teufel_stream_t s) {
+    if (!pos) return TEUFEL_ERR_ARG;
+    return teufel_cuda_integrate_screen_ex(traj, pos, &t0, dt, Nt, 1, out, nullptr, s);
+}
+
+int teufel_cuda_last_inwindow(const teufel_traj_set* traj, int64_t* inwindow,
+                              int64_t* fallback_points) {
+    if (!traj) return TEUFEL_ERR_ARG;
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj);
+    unsigned int mask = 0;
+    // device-pointer calls return before the counters are read back
+    if (cudaDeviceSynchronize() != cudaSuccess) return cuda_fail(cudaGetLastError());
+    if (h->d_counters &&
+        (cudaMemcpy(h->last_counters, h->d_counters, sizeof(h->last_counters),
+                    cudaMemcpyDeviceToHost) != cudaSuccess ||
+         cudaMemcpy(&mask, h->d_status, sizeof(mask), cudaMemcpyDeviceToHost) != cudaSuccess))
+        return cuda_fail(cudaGetLastError());
+    if (inwindow) *inwindow = (int64_t)h->last_counters[0];
+    if (fallback_points) *fallback_points = (int64_t)h->last_counters[1];
+    return status_from_mask(mask);
+}
+
+int teufel_cuda_point_decisions(const teufel_traj_set* traj, int m, const double* pos, double t0,
+                                double dt, int Nt, int64_t* idx, int* flags, double* u_est) {
+    if (!traj || !pos || !idx || !flags || !u_est || m < 0 || m >= traj->dev.n_particles ||
+        Nt < 0 || !(dt != 0.0))
+        return TEUFEL_ERR_ARG;
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj);
+    std::vector<int64_t> offs(2);
+    TRY_CUDA(cudaMemcpy(offs.data(), h->dev.offsets + m, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    int64_t n = offs[1] - offs[0];
+    if (n <= 0) return TEUFEL_OK;
+    int64_t* d_idx = nullptr;
+    int* d_flags = nullptr;
+    double* d_u = nullptr;
+    TRY_CUDA(cudaMalloc(&d_idx, sizeof(int64_t) * n));
+    TRY_CUDA(cudaMalloc(&d_flags, sizeof(int) * n));
+    TRY_CUDA(cudaMalloc(&d_u, sizeof(double) * n));
+    cudaError_t e = launch_point_decisions(h->dev, m, make_double3(pos[0], pos[1], pos[2]), t0, dt,
+                                           Nt, d_idx, d_flags, d_u, h->d_status, 0);
+    if (!e) e = cudaMemcpy(idx, d_idx, sizeof(int64_t) * n, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(flags, d_flags, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(u_est, d_u, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d_idx);
+    cudaFree(d_flags);
+    cudaFree(d_u);
+    return e ? cuda_fail(e) : TEUFEL_OK;
+}
+
+int teufel_cuda_deposit_injected(int n_particles, const int* n_points, const double* ts,
+                                 const double* f, double t0, double dt, int Nt, int precision,
+                                 double* trace) {
+    if (n_particles < 0 || Nt < 0 || (n_particles > 0 && !n_points) || !trace ||
+        (precision != TEUFEL_PREC_FP32_SPLIT && precision != TEUFEL_PREC_FP64))
+        return TEUFEL_ERR_ARG;
+    int rc = check_device();
+    if (rc) return rc;
+    std::vector<int64_t> offs(n_particles + 1, 0);
+    for (int m = 0; m < n_particles; m++) {
+        if (n_points[m] < 0) return TEUFEL_ERR_ARG;
+        offs[m + 1] = offs[m] + n_points[m];
+    }
+    int64_t N = offs[n_particles];
+    if (Nt < 2) return TEUFEL_OK;
+    if (N > 0 && (!ts || !f)) return TEUFEL_ERR_ARG;
+    int64_t* d_off = nullptr;
+    double *d_ts = nullptr, *d_f = nullptr, *d_tr = nullptr;
+    unsigned int* d_st = nullptr;
+    TRY_CUDA(cudaMalloc(&d_off, sizeof(int64_t) * (n_particles + 1)));
+    TRY_CUDA(cudaMalloc(&d_ts, sizeof(double) * (N + 1)));
+    TRY_CUDA(cudaMalloc(&d_f, sizeof(double) * 6 * (N + 1)));
+    TRY_CUDA(cudaMalloc(&d_tr, sizeof(double) * 6 * Nt));
+    TRY_CUDA(cudaMalloc(&d_st, sizeof(unsigned int)));
+    cudaError_t e = cudaMemcpy(d_off, offs.data(), sizeof(int64_t) * (n_particles + 1),
+                               cudaMemcpyHostToDevice);
+    if (!e && N) e = cudaMemcpy(d_ts, ts, sizeof(double) * N, cudaMemcpyHostToDevice);
+    if (!e && N) e = cudaMemcpy(d_f, f, sizeof(double) * 6 * N, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_tr, trace, sizeof(double) * 6 * Nt, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemset(d_st, 0, sizeof(unsigned int));
+    if (!e) e = launch_deposit_injected(n_particles, d_off, d_ts, d_f, t0, dt, Nt, precision, d_tr,
+                                        d_st, 0);
+    unsigned int mask = 0;
+    if (!e) e = cudaMemcpy(trace, d_tr, sizeof(double) * 6 * Nt, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(&mask, d_st, sizeof(mask), cudaMemcpyDeviceToHost);
+    cudaFree(d_off);
+    cudaFree(d_ts);
+    cudaFree(d_f);
+    cudaFree(d_tr);
+    cudaFree(d_st);
+    if (e) return cuda_fail(e);
+    return status_from_mask(mask);
+}
+
+int teufel_cuda_probe_peaks(double* fp32_tflops, double* fp64_tflops) {
+    int rc = check_device();
+    if (rc) return rc;
+    return probe_peaks(fp32_tflops, fp64_tflops) ? TEUFEL_ERR_CUDA : TEUFEL_OK;
+}
+
+}  // extern "C"
