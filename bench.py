@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Lienard-Wiechert field integration.
+
+Metric: particle x step x pixel evaluations per second of the FP32-split
+kernel (every step of every particle against every pixel counts, in window
+or not), on the 1e5-particle coherent-emission screen: 200 x 200 pixels over
+0.4 x 0.4 m at z = 20 m, 4096 x 2 fs traces, gamma = 300 bunch in a
+lambda_u = 0.3 m, 20-period, K = 3 undulator at 100 steps per period.
+One step integrates one batch of particles of that bunch onto the whole
+screen; every step uses a different batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank integrates a
+contiguous block of pixels (pixel shards need no exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle·step·pixel evals/s: FP32 split vs FP64 GPU at ≤1e-5 rel L2 vs FP64"
+UNIT = "evals/s"
+# algorithmic flops per in-window (pixel, particle, step) and per extra bin
+# of a multi-bin step (one LW field evaluation 89 + single-bin deposit 21)
+FLOPS_PER_STEP = 110.0
+FLOPS_PER_EXTRA_BIN = 14.0
+# dram bytes per launch of lw_fp32_kernel at the default batch, from the ncu
+# capture summarised in profiles/lw_fp32_kernel_config4.md (None until measured)
+TRAFFIC_PER_LAUNCH = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=1024, help="particles per step")
+    ap.add_argument("--pixels", type=int, default=0,
+                    help="integrate an evenly spaced subset of about this many pixels (0 = all)")
+    ap.add_argument("--slots", type=int, default=0,
+                    help="particle-range slots per launch (0 = library default)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(batch, n_pix, nots, npts, extra=None):
+    c = {"workload": "config4: 1e5-particle 200 pC bunch (sigma_z 100 um, sigma_xy 1 mm, "
+                     "gamma 300 +- 0.05%) in a lambda_u=0.3 m, 20-period, K=3 undulator at "
+                     "100 steps/period; 200x200-pixel screen over 0.4x0.4 m at z=20 m; "
+                     "4096 x 2 fs E/B traces; one step = one batch of the bunch onto the "
+                     "whole screen",
+         "particles_per_step": batch, "points_per_particle": npts, "pixels": n_pix,
+         "samples": nots, "bunch_particles": 100000,
+         "l2": "no flush: every step reads a new trajectory batch (~"
+               f"{batch * npts * 160 / 1e6:.0f} MB) and writes {n_pix * nots * 48 / 1e9:.1f} GB "
+               "of FP64 traces, both larger than the 129 MB L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [ln.strip().split(",") for ln in self.f.read().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for k, n in enumerate(names):
+                    if r[5 + k].strip().lower() in ("active", "1"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
+def make_batches(n_batches, batch, nthreads=0):
+    from teufel_gb300 import harness as H
+    out = []
+    for b in range(n_batches):
+        first = (b * batch) % 100000
+        out.append(H.config4(first=first, count=batch, nthreads=nthreads))
+    return out
+
+
+def shard(n, rank, world):
+    lo = n * rank // world
+    hi = n * (rank + 1) // world
+    return lo, hi
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline / reference arm
+# ---------------------------------------------------------------------------
+def cpu_rate(w, target_s, nthreads):
+    """Time the CPU oracle on a pixel x particle sample of workload w; the
+    sample grows until one run takes at least target_s seconds."""
+    from oracle import lw
+    from teufel_gb300 import harness as H
+    rng = np.random.default_rng(11)
+    npts = int(w.traj.n_points[0])
+    n_pix, n_part = max(nthreads, 4), 4
+    while True:
+        pix = np.sort(rng.choice(w.n_pix, min(n_pix, w.n_pix), replace=False))
+        sub = w.traj.subset(list(range(min(n_part, w.traj.n_particles))))
+        t = time.perf_counter()
+        _, rc = lw.integrate_screen(sub, w.pix_pos[pix], w.pix_t0[pix], w.dt, w.nots,
+                                    nthreads=nthreads)
+        el = time.perf_counter() - t
+        evals = len(pix) * sub.n_particles * (npts - 1)
+        if el >= target_s or (n_part >= w.traj.n_particles and n_pix >= w.n_pix):
+            return evals / el, f"{len(pix)} random pixels x {sub.n_particles} particles x " \
+                               f"{npts - 1} steps ({evals:.3g} evals, {el:.1f} s)", el
+        grow = max(2.0, min(8.0, 1.5 * target_s / max(el, 1e-3)))
+        if n_part < w.traj.n_particles:
+            n_part = min(w.traj.n_particles, int(math.ceil(n_part * grow)))
+        else:
+            n_pix = min(w.n_pix, int(math.ceil(n_pix * grow)))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import lw
+    lw.build(with_reference=False)
+    nthreads = os.cpu_count() or 1
+    w = make_batches(1, args.batch)[0]
+    npts = int(w.traj.n_points[0])
+    budget = max(2.0, 150.0 / (args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_rate(w, min(1.0, budget), nthreads)
+    rates, times, sample = [], [], ""
+    for _ in range(args.steps):
+        r, sample, el = cpu_rate(w, budget, nthreads)
+        rates.append(r)
+        times.append(el)
+    value = statistics.median(rates)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * statistics.median(times), "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.batch, w.n_pix, w.nots, npts),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": sample + " per step; the oracle's C restatement of "
+                             "ChargedParticle::integrateFieldTrace with an OpenMP pixel loop "
+                             "(the reference's own build needs its source tree, absent here)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+    from teufel_gb300 import abi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def barrier_sync():
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+
+    K, W = args.steps, max(args.warmup, 0)
+    n_batches = min(K + W, 64)
+    batches = make_batches(n_batches, args.batch)
+    if args.pixels:
+        stride = max(1, batches[0].n_pix // args.pixels)
+        batches = [b.pixel_subset(np.arange(0, b.n_pix, stride)) for b in batches]
+    w0 = batches[0]
+    npts = int(w0.traj.n_points[0])
+    lo, hi = shard(w0.n_pix, rank, world)
+    n_pix = hi - lo
+    nots = w0.nots
+    pos = torch.from_numpy(np.ascontiguousarray(w0.pix_pos[lo:hi])).to(dev)
+    t0 = torch.from_numpy(np.ascontiguousarray(w0.pix_t0[lo:hi])).to(dev)
+    out = torch.zeros((n_pix, nots, 6), dtype=torch.float64, device=dev)
+    sets = [abi.TrajSet(b.traj) for b in batches]
+    evals_step = n_pix * args.batch * (npts - 1)
+
+    def step(j, timing):
+        sets[j % n_batches].integrate_screen_device(pos.data_ptr(), t0.data_ptr(), w0.dt, nots,
+                                                    n_pix, out.data_ptr(), stream=sptr,
+                                                    timing=timing, n_slots=args.slots)
+
+    peak32, peak64 = abi.probe_peaks()
+    for j in range(W):
+        step(j, False)
+    barrier_sync()
+    clocks = Clocks(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    kernel_ms, reduce_ms, launches = 0.0, 0.0, 0
+    deposits, inwin, fallbacks = 0, 0, 0
+    barrier_sync()
+    e0.record(stream)
+    for j in range(W, W + K):
+        step(j, True)
+        d, nl, km, rm = sets[j % n_batches].last_timing()
+        iw, fb, st = sets[j % n_batches].last_inwindow()
+        abi.check(st, "integration")
+        kernel_ms += km
+        reduce_ms += rm
+        launches += nl
+        deposits += d
+        inwin += iw
+        fallbacks += fb
+    e1.record(stream)
+    barrier_sync()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ms_all = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(ms_all, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_all.item())
+    value = evals_step * world * K / (ms_max / 1e3)
+    flops = FLOPS_PER_STEP * inwin + FLOPS_PER_EXTRA_BIN * max(deposits - inwin, 0)
+    achieved = flops / (kernel_ms / 1e3) / 1e12 if kernel_ms > 0 else 0.0
+
+    # FP64 device path and accuracy on a pixel subset of the first batch
+    sub = np.arange(lo, hi, 16)
+    ws = w0.pixel_subset(sub)
+    comp = {}
+    with abi.TrajSet(ws.traj) as ts:
+        for prec, name in ((abi.PREC_FP64, "fp64"), (abi.PREC_FP32_SPLIT, "fp32")):
+            ts.integrate_screen(ws.pix_pos, ws.pix_t0, ws.dt, ws.nots, precision=prec)
+            torch.cuda.synchronize(dev)
+            reps = 2
+            tt = time.perf_counter()
+            for _ in range(reps):
+                res = ts.integrate_screen(ws.pix_pos, ws.pix_t0, ws.dt, ws.nots, precision=prec)
+            el = (time.perf_counter() - tt) / reps
+            comp[name] = (res, el)
+    ev_sub = len(sub) * args.batch * (npts - 1)
+    fp64_rate = ev_sub / comp["fp64"][1]
+    fp32_rate_sub = ev_sub / comp["fp32"][1]
+    ref64 = comp["fp64"][0]
+    rel = float(np.linalg.norm(comp["fp32"][0] - ref64) / np.linalg.norm(ref64))
+    peak_err = float(np.abs(comp["fp32"][0] - ref64).max() / np.abs(ref64).max())
+
+    # end to end through the C-ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        out_h = torch.zeros((n_pix, nots, 6), dtype=torch.float64).pin_memory().numpy()
+        pos_h = torch.from_numpy(np.ascontiguousarray(w0.pix_pos[lo:hi])).pin_memory().numpy()
+        t0_h = torch.from_numpy(np.ascontiguousarray(w0.pix_t0[lo:hi])).pin_memory().numpy()
+        pinned = []
+        for b in batches[:min(n_batches, K)]:
+            tr = b.traj
+            pinned.append(tuple(torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+                                for a in (tr.n_points.astype(np.int32), tr.charge, tr.t, tr.x,
+                                          tr.p, tr.a)))
+        h2d = 0
+        d2h = n_pix * nots * 48
+        barrier_sync()
+        tt = time.perf_counter()
+        for j in range(K):
+            npnt, ch, t, x, p, a = pinned[j % len(pinned)]
+            with abi.TrajSet.from_arrays(npnt, ch, t, x, p, a) as ts:
+                ts.integrate_screen(pos_h, t0_h, w0.dt, nots, out=out_h)
+            if j == 0:
+                h2d = sum(v.nbytes for v in (npnt, ch, t, x, p, a)) + pos_h.nbytes + \
+                    t0_h.nbytes + out_h.nbytes
+        barrier_sync()
+        el = time.perf_counter() - tt
+        el_all = torch.tensor([el], dtype=torch.float64, device=dev)
+        if dist:
+            dist.all_reduce(el_all, op=dist.ReduceOp.MAX)
+        e2e = {"value": evals_step * world * K / float(el_all.item()), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": 1e3 * float(el_all.item()) / K}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        rate, sample, _ = cpu_rate(w0, 12.0, nthreads)
+        cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": sample + "; the oracle's C restatement of the reference's "
+                         "integrateFieldTrace, OpenMP over pixels"}
+
+    if rank == 0:
+        frac_in = inwin / (evals_step * K) if K else 0.0
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args.batch, w0.n_pix, nots, npts,
+                                      {"parallelism": f"pixel shards x{world}",
+                                       "in_window_fraction": frac_in,
+                                       "exact_fallback_points": fallbacks}),
+            "fp64_gpu": {"value": fp64_rate, "unit": UNIT,
+                         "sample": f"{len(sub)} pixels (every 16th) x {args.batch} particles",
+                         "fp32_split_same_sample": fp32_rate_sub,
+                         "speedup_fp32_split_over_fp64": fp32_rate_sub / fp64_rate},
+            "accuracy": {"rel_l2_fp32_split_vs_fp64": rel, "peak_sample_rel_err": peak_err,
+                         "sample": f"{len(sub)} pixels x {args.batch} particles"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32,
+                         "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,
+                         "traffic": TRAFFIC_PER_LAUNCH,
+                         "kernel": "lw_fp32_kernel",
+                         "peak_source": "FFMA throughput probe run by bench.py on this GPU "
+                                        "(MEASURED_PEAKS.json has no FP32 figure)",
+                         "algorithmic_flops": flops, "kernel_ms": kernel_ms,
+                         "reduce_ms": reduce_ms, "fp64_probe_tflops": peak64},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    for s in sets:
+        s.free()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -63,6 +63,8 @@ typedef struct teufel_options {
     int device_pointers;  /* 1: pix_pos, pix_t0 and out are device pointers      */
     int n_slots;          /* particle-range slots reduced in FP64; 0 = automatic  */
     int threads_per_block;/* 0 = automatic (128)                                 */
+    int timing;           /* 1: time the kernels with CUDA events on the stream,
+                             read back by teufel_cuda_last_timing               */
 } teufel_options;
 
 /* Fill *opt with the defaults (FP32 split path, host pointers, automatic tiling). */
@@ -139,6 +141,14 @@ int teufel_cuda_deposit_injected(int n_particles, const int *n_points, const dou
  * the trace window (the reference's condition at src/particle.cpp:793). */
 int teufel_cuda_last_inwindow(const teufel_traj_set *traj, int64_t *inwindow,
                               int64_t *fallback_points);
+
+/* Work and timing of the last integrate call on this handle: deposits =
+ * bin contributions made (>= in-window steps; multi-bin steps add one per
+ * extra bin), launches = kernels launched, and -- when it ran with
+ * options.timing -- the summed CUDA-event durations of the integration
+ * kernels and of the reduction kernels [ms].  Synchronizes the device. */
+int teufel_cuda_last_timing(const teufel_traj_set *traj, int64_t *deposits, int *launches,
+                            double *kernel_ms, double *reduce_ms);
 
 /* Peak FP32 FMA throughput of the current device measured with a dependent-
  * free FFMA kernel (TFLOP/s, FMA = 2 flops), and the same for FP64 DFMA. */

@@ -56,6 +56,9 @@ def oracle():
         L.lwo_integrate_screen.restype = ctypes.c_int
         L.lwo_integrate_screen.argtypes = [_i64, _lp, _dp, _dp, _dp, _dp, _dp, _i64, _dp, _dp,
                                            ctypes.c_double, _i64, _dp, ctypes.c_int, _lp]
+        L.lwo_integrate_screen_ext.restype = ctypes.c_int
+        L.lwo_integrate_screen_ext.argtypes = [_i64, _lp, _dp, _dp, _dp, _dp, _dp, _i64, _dp,
+                                               _dp, ctypes.c_double, _i64, _dp, ctypes.c_int]
         L.lwo_deposit_injected.restype = ctypes.c_int
         L.lwo_deposit_injected.argtypes = [_i64, _lp, _dp, _dp, ctypes.c_double,
                                            ctypes.c_double, _i64, _dp]
@@ -105,7 +108,11 @@ def integrate_screen(traj, pix_pos, pix_t0, dt, nots, out=None, nthreads=0, impl
     offs = _c(traj.offsets, np.int64)
     t, x, p, a = _c(traj.t), _c(traj.x), _c(traj.p), _c(traj.a)
     ch = _c(traj.charge)
-    if impl == "oracle":
+    if impl == "extended":
+        rc = oracle().lwo_integrate_screen_ext(traj.n_particles, _p(offs, _lp), _p(ch), _p(t),
+                                               _p(x), _p(p), _p(a), n_pix, _p(pix_pos),
+                                               _p(pix_t0), dt, nots, _p(out), nthreads)
+    elif impl == "oracle":
         touched = ctypes.c_int64(0)
         rc = oracle().lwo_integrate_screen(traj.n_particles, _p(offs, _lp), _p(ch), _p(t), _p(x),
                                            _p(p), _p(a), n_pix, _p(pix_pos), _p(pix_t0), dt,

@@ -255,6 +255,52 @@ int lwo_integrate_screen(int64_t n_part, const int64_t *offsets, const double *c
     return err_all;
 }
 
+/* The same integration with arrival times evaluated in long double (64-bit
+   significand on x86-64, 113 bits on aarch64) and deposited in bin units:
+   an accuracy reference for cases where the FP64 flight time's own rounding
+   matters (attosecond bins 30 m from the source).  Fields are the FP64
+   restatement.  Bins and weights follow lwo_deposit_step with t0 = 0, dt = 1
+   on u = (ts - t0)/dt. */
+int lwo_integrate_screen_ext(int64_t n_part, const int64_t *offsets, const double *charge,
+                             const double *t, const double *x, const double *bg, const double *a,
+                             int64_t n_pix, const double *pix_pos, const double *pix_t0,
+                             double dt, int64_t nots, double *out, int nthreads)
+{
+    int err_all = LWO_OK;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(static)
+    for (int64_t ip = 0; ip < n_pix; ip++) {
+        int err = LWO_OK;
+        const double *obs = pix_pos + 3 * ip;
+        double *trace = out + 6 * nots * ip;
+        for (int64_t m = 0; m < n_part && nots >= 2; m++) {
+            int64_t o = offsets[m], np = offsets[m + 1] - o;
+            if (np < 2) continue;
+            double u1 = 0.0, f1[6], f2[6];
+            for (int64_t i = 0; i < np; i++) {
+                const double *xi = x + 3 * (o + i);
+                long double rx = (long double)obs[0] - xi[0];
+                long double ry = (long double)obs[1] - xi[1];
+                long double rz = (long double)obs[2] - xi[2];
+                long double R = sqrtl(rx * rx + ry * ry + rz * rz);
+                long double ts = (long double)t[o + i] + R / (long double)LWO_C;
+                double u2 = (double)((ts - (long double)pix_t0[ip]) / (long double)dt);
+                lwo_retarded_field(xi, bg + 3 * (o + i), a + 3 * (o + i), charge[m], obs, f2);
+                if (i > 0) lwo_deposit_step(u1, u2, f1, f2, 0.0, 1.0, nots, trace, &err);
+                u1 = u2;
+                memcpy(f1, f2, sizeof f1);
+            }
+        }
+        if (err != LWO_OK) {
+#pragma omp critical
+            { if (err_all == LWO_OK) err_all = err; }
+        }
+    }
+    return err_all;
+}
+
 /* Deposit-only entry for the known-answer test: particle m has np[m] points
    with given arrival times ts and fields f[6] (what the reference's KAT
    injects by overriding RetardedTime/RetardedField). */

@@ -33,7 +33,7 @@ CUDA_LIB = LIBDIR / "libteufel_gb300.so"
 HARNESS_LIB = LIBDIR / "libteufel_harness.so"
 
 CU_SOURCES = ["teufel_abi.cu", "lw_fp64.cu", "lw_fp32.cu", "lw_support.cu"]
-CU_HEADERS = ["lw_common.cuh", "lw_deposit.cuh", "lw_internal.h"]
+CU_HEADERS = ["lw_common.cuh", "lw_internal.h"]
 
 
 def _newer(out: Path, deps) -> bool:

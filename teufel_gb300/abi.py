@@ -30,13 +30,14 @@ EXPORTED = [
     "teufel_cuda_traj_free", "teufel_cuda_traj_points", "teufel_cuda_integrate_screen",
     "teufel_cuda_integrate_point", "teufel_cuda_integrate_screen_ex",
     "teufel_cuda_point_decisions", "teufel_cuda_deposit_injected", "teufel_cuda_last_inwindow",
-    "teufel_cuda_probe_peaks",
+    "teufel_cuda_probe_peaks", "teufel_cuda_last_timing",
 ]
 
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device_pointers", ctypes.c_int),
-                ("n_slots", ctypes.c_int), ("threads_per_block", ctypes.c_int)]
+                ("n_slots", ctypes.c_int), ("threads_per_block", ctypes.c_int),
+                ("timing", ctypes.c_int)]
 
 
 class TeufelError(RuntimeError):
@@ -93,6 +94,8 @@ def lib():
                                                    _dp]
         L.teufel_cuda_last_inwindow.restype = ctypes.c_int
         L.teufel_cuda_last_inwindow.argtypes = [_vp, _lp, _lp]
+        L.teufel_cuda_last_timing.restype = ctypes.c_int
+        L.teufel_cuda_last_timing.argtypes = [_vp, _lp, _ip, _dp, _dp]
         L.teufel_cuda_probe_peaks.restype = ctypes.c_int
         L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp]
         _lib = L
@@ -118,12 +121,13 @@ def _ptr(a, t=_dp):
 
 
 def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
-            n_slots: int = 0) -> Options:
+            n_slots: int = 0, timing: bool = False) -> Options:
     o = Options()
     lib().teufel_cuda_default_options(ctypes.byref(o))
     o.precision = precision
     o.device_pointers = 1 if device_pointers else 0
     o.n_slots = n_slots
+    o.timing = 1 if timing else 0
     return o
 
 
@@ -196,9 +200,9 @@ class TrajSet:
 
     def integrate_screen_device(self, pos_ptr: int, t0_ptr: int, dt: float, nots: int,
                                 n_pix: int, out_ptr: int, precision: int = PREC_FP32_SPLIT,
-                                n_slots: int = 0, stream: int = 0) -> None:
+                                n_slots: int = 0, stream: int = 0, timing: bool = False) -> None:
         """Device-pointer variant; returns once the work is enqueued."""
-        opt = options(precision, True, n_slots)
+        opt = options(precision, True, n_slots, timing)
         check(lib().teufel_cuda_integrate_screen_ex(self.handle, _vp(pos_ptr), _vp(t0_ptr), dt,
                                                     nots, n_pix, _vp(out_ptr),
                                                     ctypes.byref(opt), _vp(stream)),
@@ -217,6 +221,18 @@ class TrajSet:
         fb = ctypes.c_int64(0)
         st = lib().teufel_cuda_last_inwindow(self.handle, ctypes.byref(iw), ctypes.byref(fb))
         return int(iw.value), int(fb.value), st
+
+    def last_timing(self):
+        """(deposits, kernel launches, integration-kernel ms, reduction ms)
+        of the last call; the times need timing=True on that call."""
+        dep = ctypes.c_int64(0)
+        nl = ctypes.c_int(0)
+        k = ctypes.c_double(0)
+        r = ctypes.c_double(0)
+        check(lib().teufel_cuda_last_timing(self.handle, ctypes.byref(dep), ctypes.byref(nl),
+                                            ctypes.byref(k), ctypes.byref(r)),
+              "teufel_cuda_last_timing")
+        return int(dep.value), int(nl.value), float(k.value), float(r.value)
 
     def point_decisions(self, m, pos, t0, dt, nots):
         n = int(self.n_points[m])

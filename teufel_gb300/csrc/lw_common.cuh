@@ -264,17 +264,20 @@ struct BinSink {
     int nt;
     T* row;  // this pixel's partial trace, [nt][STRIDE]
     unsigned int err;
+    unsigned long long n_add;
     __device__ void init(T* r, int n) {
         row = r;
         nt = n;
         open = -1;
         err = 0;
+        n_add = 0;
     }
     __device__ __forceinline__ void add(int k, const T* f) {
         if (k < 0 || k >= nt) {
             err |= 1u << TEUFEL_ERR_RANGE;
             return;
         }
+        n_add++;
         if (k == open) {
 #pragma unroll
             for (int c = 0; c < 6; c++) a[c] += f[c];

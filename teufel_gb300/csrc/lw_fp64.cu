@@ -123,7 +123,11 @@ __global__ void __launch_bounds__(128)
     sink.flush();
     if (sink.err) atomicOr(wk.status, sink.err);
     inwin = warp_sum_u64(inwin);
-    if ((threadIdx.x & 31) == 0 && wk.counters && inwin) atomicAdd(wk.counters, inwin);
+    unsigned long long nadd = warp_sum_u64(sink.n_add);
+    if ((threadIdx.x & 31) == 0 && wk.counters) {
+        if (inwin) atomicAdd(wk.counters, inwin);
+        if (nadd) atomicAdd(wk.counters + 2, nadd);
+    }
 }
 
 cudaError_t launch_fp64(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,

@@ -16,7 +16,7 @@ constexpr double kEps0 = 8.854187817e-12;
 // Trajectory points are grouped into segments of kSegLen steps.  Segment k of
 // a particle owns steps [k*kSegLen, (k+1)*kSegLen) and its first point is the
 // FP64 anchor from which the FP32 path measures positions and arrival times.
-constexpr int kSegShift = 6;
+constexpr int kSegShift = 5;
 constexpr int kSegLen = 1 << kSegShift;
 
 // Device view of a resident trajectory set.
@@ -31,10 +31,11 @@ struct DevTraj {
     const double4_32a* tx;          // [Npts] t, x, y, z                 (FP64, as uploaded)
     const double4_32a* pp;          // [Npts] beta*gamma, w unused        (FP64)
     const double4_32a* aa;          // [Npts] d(beta*gamma)/dt, w unused  (FP64)
-    const float4* q0;           // [Npts] e = x - x_anchor (xyz), dtau = (t - t_a) - vhat.e/c
+    const float4* q0;           // [Npts] e = x - x_anchor (xyz), duration of the step from here
     const float4* q1;           // [Npts] beta-hat (xyz), eps = 1 - |beta|
     const float4* q2;           // [Npts] A/gamma*scale/c (xyz), scale/gamma^2
-    const float4* segb;         // [Nseg] max|dtau|, max|vhat.e|, max|e_perp|, max|e|
+    const float4* q3;           // [Npts] chord direction of the step from here (xyz),
+                                //        1 - |chord velocity|/c
 };
 
 // One observer handed to a kernel launch.
@@ -53,7 +54,8 @@ struct DevWork {
     void* scratch;            // per-slot partial traces
     int64_t slot_stride;      // elements between slots
     unsigned int* status;     // bit mask of TEUFEL_ERR_* seen on the device
-    unsigned long long* counters;  // [0] in-window triples, [1] exact-fallback points
+    unsigned long long* counters;  // [0] in-window triples, [1] exact-fallback points,
+                                   // [2] bin contributions (deposits)
 };
 
 }  // namespace teufel
@@ -69,11 +71,15 @@ cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* ou
 cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* out,
                                cudaStream_t s);
 cudaError_t launch_point_decisions(const DevTraj& tr, int m, double3 pos, double t0, double dt,
-                                   int nt, int64_t* idx, int* flags, double* u_est,
-                                   unsigned int* status, cudaStream_t s);
+                                   int nt, int64_t n_points, int64_t* idx, int* flags,
+                                   double* u_est, cudaStream_t s);
 cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const double* ts,
                                     const double* f, double t0, double dt, int nt, int precision,
                                     double* trace, unsigned int* status, cudaStream_t s);
 cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s);
+cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const double* ts,
+                                      const double* f, double t0, double dt, int nt,
+                                      double* trace, float* trace32, unsigned int* status,
+                                      cudaStream_t s);
 int probe_peaks(double* fp32_tflops, double* fp64_tflops);
 }  // namespace teufel

@@ -89,16 +89,16 @@ cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* ou
 // Deposit of injected (ts, field) sequences: the reference's known-answer
 // test replaces RetardedTime/RetardedField by fixed values
 // (tests/teufel.integrate_field.cpp:51-78); this runs the device deposit on
-// such values.  One thread, particles in order.
+// such values (FP64 path; the FP32 path's routine is in lw_fp32.cu).  One
+// thread, particles in order.
 // ---------------------------------------------------------------------------
 __global__ void deposit_injected_kernel(int n_part, const int64_t* offs, const double* ts,
                                         const double* f, double t0, double dt, int nt,
-                                        int precision, double* trace, float* trace32,
-                                        unsigned int* status) {
+                                        double* trace, unsigned int* status) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     Window w = make_window(t0, dt, nt);
     unsigned int err = 0;
-    if (precision == TEUFEL_PREC_FP64) {
+    {
         BinSink<double, 6> sink;
         sink.init(trace, nt);
         Geo64 geo{t0, dt};
@@ -113,27 +113,6 @@ __global__ void deposit_injected_kernel(int n_part, const int64_t* offs, const d
         }
         sink.flush();
         err = sink.err;
-    } else {
-        BinSink<float, 6> sink;
-        sink.init(trace32, nt);
-        Geo32 geo{0};
-        for (int m = 0; m < n_part; m++) {
-            int64_t o = offs[m], n = offs[m + 1] - o;
-            for (int64_t s = 0; s + 1 < n; s++) {
-                double a = ts[o + s], b = ts[o + s + 1];
-                float f1[6], f2[6];
-                for (int c = 0; c < 6; c++) {
-                    f1[c] = (float)f[6 * (o + s) + c];
-                    f2[c] = (float)f[6 * (o + s + 1) + c];
-                }
-                deposit_step<Ops32>((float)((a - t0) / dt), (float)((b - t0) / dt),
-                                    exact_bin(a, w), exact_flags(a, w), exact_bin(b, w),
-                                    exact_flags(b, w), f1, f2, geo, nt, sink);
-            }
-        }
-        sink.flush();
-        err = sink.err;
-        for (int k = 0; k < 6 * nt; k++) trace[k] += (double)trace32[k];
     }
     if (err) atomicOr(status, err);
 }
@@ -145,9 +124,12 @@ cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const doubl
     cudaError_t e = cudaMallocAsync(&t32, sizeof(float) * 6 * (size_t)(nt > 0 ? nt : 1), s);
     if (e != cudaSuccess) return e;
     cudaMemsetAsync(t32, 0, sizeof(float) * 6 * (size_t)(nt > 0 ? nt : 1), s);
-    deposit_injected_kernel<<<1, 32, 0, s>>>(n_part, offs, ts, f, t0, dt, nt, precision, trace,
-                                             t32, status);
-    e = cudaGetLastError();
+    if (precision == TEUFEL_PREC_FP64) {
+        deposit_injected_kernel<<<1, 32, 0, s>>>(n_part, offs, ts, f, t0, dt, nt, trace, status);
+        e = cudaGetLastError();
+    } else {
+        e = launch_deposit_injected32(n_part, offs, ts, f, t0, dt, nt, trace, t32, status, s);
+    }
     cudaFreeAsync(t32, s);
     return e;
 }

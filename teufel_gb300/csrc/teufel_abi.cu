@@ -33,7 +33,12 @@ struct teufel_traj_set {
     size_t out_cap = 0;  // doubles
     unsigned int* d_status = nullptr;
     unsigned long long* d_counters = nullptr;
-    unsigned long long last_counters[2] = {0, 0};
+    unsigned long long last_counters[3] = {0, 0, 0};
+    // kernel timing of the last call (options.timing)
+    std::vector<cudaEvent_t> ev;
+    int n_ev_used = 0;
+    int last_launches = 0;
+    bool last_timed = false;
     std::vector<int64_t> h_seg_offsets;
 };
 
@@ -161,7 +166,18 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     TRY_CUDA(cudaMemcpyAsync(h->slot_seg, bounds.data(), sizeof(int64_t) * (slots_total + 1),
                              cudaMemcpyHostToDevice, s));
     TRY_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), s));
-    TRY_CUDA(cudaMemsetAsync(h->d_counters, 0, 2 * sizeof(unsigned long long), s));
+    TRY_CUDA(cudaMemsetAsync(h->d_counters, 0, 3 * sizeof(unsigned long long), s));
+    h->n_ev_used = 0;
+    h->last_launches = 0;
+    h->last_timed = opt.timing != 0;
+    const int64_t n_passes = (slots_total + per_pass - 1) / per_pass;
+    if (h->last_timed && (int64_t)h->ev.size() < 4 * n_passes) {
+        while ((int64_t)h->ev.size() < 4 * n_passes) {
+            cudaEvent_t e;
+            TRY_CUDA(cudaEventCreate(&e));
+            h->ev.push_back(e);
+        }
+    }
     DevScreen sc{d_pos, d_t0, np, nt, dt};
     for (int64_t p0 = 0; p0 < slots_total; p0 += per_pass) {
         DevWork w;
@@ -171,11 +187,18 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         w.slot_stride = (int64_t)np * nt * 6;
         w.status = h->d_status;
         w.counters = h->d_counters;
+        if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used], s));
         cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
                              : launch_fp32(h->dev, sc, w, kThreads, s);
         if (e != cudaSuccess) return cuda_fail(e);
+        if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 1], s));
         e = fp64 ? launch_reduce_fp64(w, sc, d_out, s) : launch_reduce_fp32(w, sc, d_out, s);
         if (e != cudaSuccess) return cuda_fail(e);
+        if (h->last_timed) {
+            TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 2], s));
+            h->n_ev_used += 4;
+        }
+        h->last_launches += 2;
     }
     return TEUFEL_OK;
 }
@@ -207,6 +230,7 @@ void teufel_cuda_default_options(teufel_options* opt) {
     opt->device_pointers = 0;
     opt->n_slots = 0;
     opt->threads_per_block = 0;
+    opt->timing = 0;
 }
 
 const char* teufel_cuda_status_string(int status) {
@@ -254,16 +278,16 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     int64_t *p_off, *p_seg;
     double* p_charge;
     double4_32a *p_vhat, *p_tx, *p_pp, *p_aa;
-    float4 *p_q0, *p_q1, *p_q2, *p_segb;
+    float4 *p_q0, *p_q1, *p_q2, *p_q3;
     if ((rc = dev_alloc(h, &p_off, n_particles + 1)) || (rc = dev_alloc(h, &p_seg, n_particles + 1)) ||
         (rc = dev_alloc(h, &p_charge, n_particles)) || (rc = dev_alloc(h, &p_vhat, n_particles)) ||
         (rc = dev_alloc(h, &p_tx, N)) || (rc = dev_alloc(h, &p_pp, N)) ||
         (rc = dev_alloc(h, &p_aa, N)) || (rc = dev_alloc(h, &p_q0, N)) ||
         (rc = dev_alloc(h, &p_q1, N)) || (rc = dev_alloc(h, &p_q2, N)) ||
-        (rc = dev_alloc(h, &p_segb, d.n_segments)))
+        (rc = dev_alloc(h, &p_q3, N)))
         return fail(rc);
     if (cudaMalloc(&h->d_status, sizeof(unsigned int)) != cudaSuccess ||
-        cudaMalloc(&h->d_counters, 2 * sizeof(unsigned long long)) != cudaSuccess)
+        cudaMalloc(&h->d_counters, 3 * sizeof(unsigned long long)) != cudaSuccess)
         return fail(cuda_fail(cudaErrorMemoryAllocation));
     d.offsets = p_off;
     d.seg_offsets = p_seg;
@@ -275,7 +299,7 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     d.q0 = p_q0;
     d.q1 = p_q1;
     d.q2 = p_q2;
-    d.segb = p_segb;
+    d.q3 = p_q3;
     cudaStream_t s = 0;
     if (cudaMemcpy(p_off, offs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
         cudaMemcpy(p_seg, segs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
@@ -323,6 +347,7 @@ int teufel_cuda_traj_free(teufel_traj_set* traj) {
     if (traj->d_out) cudaFree(traj->d_out);
     if (traj->d_status) cudaFree(traj->d_status);
     if (traj->d_counters) cudaFree(traj->d_counters);
+    for (cudaEvent_t e : traj->ev) cudaEventDestroy(e);
     delete traj;
     return TEUFEL_OK;
 }
@@ -341,7 +366,9 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     if (opt_in) opt = *opt_in;
     if (opt.precision != TEUFEL_PREC_FP32_SPLIT && opt.precision != TEUFEL_PREC_FP64)
         return TEUFEL_ERR_ARG;
-    h->last_counters[0] = h->last_counters[1] = 0;
+    h->last_counters[0] = h->last_counters[1] = h->last_counters[2] = 0;
+    h->last_launches = 0;
+    h->n_ev_used = 0;
     // the reference returns early for traces shorter than 2 samples and for
     // trajectories shorter than 2 points (src/particle.cpp:778, 783)
     if (Nt < 2 || Np == 0 || h->dev.n_particles == 0 || h->dev.n_segments == 0) return TEUFEL_OK;
@@ -398,6 +425,32 @@ int teufel_cuda_last_inwindow(const teufel_traj_set* traj, int64_t* inwindow,
     return status_from_mask(mask);
 }
 
+int teufel_cuda_last_timing(const teufel_traj_set* traj, int64_t* deposits, int* launches,
+                            double* kernel_ms, double* reduce_ms) {
+    if (!traj) return TEUFEL_ERR_ARG;
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj);
+    if (cudaDeviceSynchronize() != cudaSuccess) return cuda_fail(cudaGetLastError());
+    if (h->d_counters && cudaMemcpy(h->last_counters, h->d_counters, sizeof(h->last_counters),
+                                    cudaMemcpyDeviceToHost) != cudaSuccess)
+        return cuda_fail(cudaGetLastError());
+    double k = 0.0, r = 0.0;
+    if (h->last_timed) {
+        for (int i = 0; i + 2 < h->n_ev_used; i += 4) {
+            float a = 0.0f, b = 0.0f;
+            if (cudaEventElapsedTime(&a, h->ev[i], h->ev[i + 1]) != cudaSuccess ||
+                cudaEventElapsedTime(&b, h->ev[i + 1], h->ev[i + 2]) != cudaSuccess)
+                return cuda_fail(cudaGetLastError());
+            k += a;
+            r += b;
+        }
+    }
+    if (deposits) *deposits = (int64_t)h->last_counters[2];
+    if (launches) *launches = h->last_launches;
+    if (kernel_ms) *kernel_ms = k;
+    if (reduce_ms) *reduce_ms = r;
+    return TEUFEL_OK;
+}
+
 int teufel_cuda_point_decisions(const teufel_traj_set* traj, int m, const double* pos, double t0,
                                 double dt, int Nt, int64_t* idx, int* flags, double* u_est) {
     if (!traj || !pos || !idx || !flags || !u_est || m < 0 || m >= traj->dev.n_particles ||
@@ -415,7 +468,7 @@ int teufel_cuda_point_decisions(const teufel_traj_set* traj, int m, const double
     TRY_CUDA(cudaMalloc(&d_flags, sizeof(int) * n));
     TRY_CUDA(cudaMalloc(&d_u, sizeof(double) * n));
     cudaError_t e = launch_point_decisions(h->dev, m, make_double3(pos[0], pos[1], pos[2]), t0, dt,
-                                           Nt, d_idx, d_flags, d_u, h->d_status, 0);
+                                           Nt, n, d_idx, d_flags, d_u, 0);
     if (!e) e = cudaMemcpy(idx, d_idx, sizeof(int64_t) * n, cudaMemcpyDeviceToHost);
     if (!e) e = cudaMemcpy(flags, d_flags, sizeof(int) * n, cudaMemcpyDeviceToHost);
     if (!e) e = cudaMemcpy(u_est, d_u, sizeof(double) * n, cudaMemcpyDeviceToHost);
