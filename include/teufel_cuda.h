@@ -78,13 +78,14 @@ const char *teufel_cuda_status_string(int status);
  * (src/particle.h:417-427) made by integrateFieldTrace.
  *   n_particles          number of particles (>= 0)
  *   n_points[n]          trajectory points per particle (NP, src/particle.h:378)
- *   charge_e[n]          ChargedParticle::Charge, in units of e (src/particle.h:388)
+ *   charge_C[n]          particle charge [C]: ChargedParticle::getCharge() (src/particle.h:115),
+ *                        i.e. Charge*ElementaryCharge as the reference forms it
  *   t[Npts]              trajectory times [s], Npts = sum(n_points), particles concatenated
  *   x[Npts][3]           positions [m]
  *   bg[Npts][3]          beta*gamma (TrajMomentum)
  *   a[Npts][3]           d(beta*gamma)/dt [1/s] (TrajAccel)
  * Non-finite inputs are rejected with TEUFEL_ERR_ARG. */
-int teufel_cuda_traj_upload(int n_particles, const int *n_points, const double *charge_e,
+int teufel_cuda_traj_upload(int n_particles, const int *n_points, const double *charge_C,
                             const double *t, const double *x, const double *bg, const double *a,
                             teufel_traj_set **out);
 

@@ -1,0 +1,283 @@
+// teufel_observers.hpp -- C++ host layer over the C-ABI (teufel_cuda.h) with
+// the interface of TEUFEL's observers, for code written against them.
+//
+// Mirrors, with the same member names, argument meaning and error behaviour:
+//   BaseObserver / Observer<SourceT>     src/observer.h:43-146
+//   ScreenObserver<Beam>                 src/screen.h, src/screen.cpp:34-146, 240-296
+//   MeshedScreen<Beam> (integrate/buffer) src/mesh.cpp:289-316, 376-425
+//   PointObserver<Beam>                  src/point_observer.cpp:30-110
+//   FieldTrace (t0, dt, N, add, buffer)  src/fieldtrace.h, src/fieldtrace.cpp
+//   IOexception                          src/global.h:75-84
+// integrate() runs on the GPU through teufel_cuda_integrate_screen /
+// teufel_cuda_integrate_point; there is no CPU path.  A non-zero status is
+// rethrown as IOexception carrying the C-ABI's message, as the reference
+// throws IOexception from FieldTrace::add for out-of-range deposits.
+//
+// The field source (the reference's Beam/Bunch) is a TrajectorySource: the
+// particles' trajectory arrays, uploaded once on first use and kept on the
+// device for every observer that integrates from it.
+#pragma once
+
+#include <cstddef>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "teufel_cuda.h"
+
+namespace teufel_gb300 {
+
+class IOexception : public std::exception {
+public:
+    explicit IOexception(std::string m) : msg(std::move(m)) {}
+    const char* what() const throw() override { return msg.c_str(); }
+
+private:
+    std::string msg;
+};
+
+inline void check_status(int st, const char* where) {
+    if (st != TEUFEL_OK)
+        throw IOexception(std::string(where) + " - " + teufel_cuda_status_string(st));
+}
+
+struct Vector {
+    double x = 0.0, y = 0.0, z = 0.0;
+    Vector() = default;
+    Vector(double a, double b, double c) : x(a), y(b), z(c) {}
+    Vector operator+(const Vector& o) const { return Vector(x + o.x, y + o.y, z + o.z); }
+    Vector operator*(double f) const { return Vector(x * f, y * f, z * f); }
+};
+
+// One electromagnetic sample: Ex, Ey, Ez, Bx, By, Bz (the ElMagField layout).
+struct ElMagField {
+    double c[6] = {0, 0, 0, 0, 0, 0};
+    Vector E() const { return Vector(c[0], c[1], c[2]); }
+    Vector B() const { return Vector(c[3], c[4], c[5]); }
+};
+
+// Trajectories of a particle set (what Beam/Bunch hold as ChargedParticle
+// Time/X/P/A arrays, src/particle.h:417-427).
+class TrajectorySource {
+public:
+    TrajectorySource() = default;
+    TrajectorySource(const TrajectorySource&) = delete;
+    TrajectorySource& operator=(const TrajectorySource&) = delete;
+    ~TrajectorySource() { release(); }
+
+    // Append one particle: charge [C] (ChargedParticle::getCharge()),
+    // n trajectory points of time [s], position [m], beta*gamma and
+    // d(beta*gamma)/dt [1/s] (TrajTime/TrajPoint/TrajMomentum/TrajAccel).
+    void Add(double charge_C, int n, const double* t, const double* x, const double* bg,
+             const double* a) {
+        release();
+        charge.push_back(charge_C);
+        npts.push_back(n);
+        T.insert(T.end(), t, t + n);
+        X.insert(X.end(), x, x + 3 * (size_t)n);
+        P.insert(P.end(), bg, bg + 3 * (size_t)n);
+        A.insert(A.end(), a, a + 3 * (size_t)n);
+    }
+    int getNOP() const { return (int)npts.size(); }
+
+    // the device-resident set, uploaded on first use
+    const teufel_traj_set* device() {
+        if (!handle)
+            check_status(teufel_cuda_traj_upload((int)npts.size(), npts.data(), charge.data(),
+                                                 T.data(), X.data(), P.data(), A.data(), &handle),
+                         "TrajectorySource::device");
+        return handle;
+    }
+    void release() {
+        if (handle) teufel_cuda_traj_free(handle);
+        handle = nullptr;
+    }
+
+private:
+    std::vector<double> charge, T, X, P, A;
+    std::vector<int> npts;
+    teufel_traj_set* handle = nullptr;
+};
+
+// FieldTrace: N samples of width dt centred on t0 + i*dt (src/fieldtrace.h).
+class FieldTrace {
+public:
+    FieldTrace(double t0_p, double dt_p, std::size_t N_p) : t0(t0_p), dt(dt_p), N(N_p), f(N_p) {}
+    double get_t0() const { return t0; }
+    double get_dt() const { return dt; }
+    std::size_t get_N() const { return N; }
+    double get_time(std::size_t i) const {
+        if (i >= N) throw IOexception("FieldTrace::get_time - index out of range.");
+        return t0 + i * dt;
+    }
+    ElMagField get_field(std::size_t i) const {
+        if (i >= N) throw IOexception("FieldTrace::get_field - index out of range.");
+        return f[i];
+    }
+    void zero() { std::fill(f.begin(), f.end(), ElMagField()); }
+    double* data() { return f.empty() ? nullptr : f[0].c; }
+
+private:
+    double t0, dt;
+    std::size_t N;
+    std::vector<ElMagField> f;
+};
+
+class BaseObserver {
+public:
+    virtual ~BaseObserver() {}
+    virtual void integrate() = 0;
+    virtual std::size_t getBufferSize() = 0;
+    virtual double* getBuffer() = 0;  // new[]-allocated, freed by the caller
+    virtual void fromBuffer(double* buffer, std::size_t size) = 0;
+};
+
+template <typename SourceT>
+class Observer : public BaseObserver {
+public:
+    virtual void setSource(SourceT* src) { source = src; }
+    SourceT* source = nullptr;
+};
+
+// Nx x Ny rectangular screen (src/screen.cpp:34-110).
+class ScreenObserver : public Observer<TrajectorySource> {
+public:
+    ScreenObserver(Vector position, Vector dx, Vector dy, unsigned int nx, unsigned int ny,
+                   double t0, double dt, double dtx, double dty, unsigned int nots)
+        : Origin(position), dX(dx), dY(dy), Nx(nx), Ny(ny), t0_obs(t0), dt_obs(dt),
+          dtx_obs(dtx), dty_obs(dty), NOTS(nots),
+          buf((std::size_t)nx * ny * nots * 6, 0.0) {}
+
+    // center index is Nx/2, Ny/2 with integer division (src/screen.cpp:97-103)
+    Vector CellPosition(unsigned int ix, unsigned int iy) const {
+        return Origin + dX * (double)((int)ix - (int)Nx / 2) + dY * (double)((int)iy - (int)Ny / 2);
+    }
+    double CellTimeZero(unsigned int ix, unsigned int iy) const {
+        return t0_obs + dtx_obs * (double)((int)ix - (int)Nx / 2) +
+               dty_obs * (double)((int)iy - (int)Ny / 2);
+    }
+
+    void integrate() override {
+        if (!source) throw IOexception("ScreenObserver::integrate - no source set");
+        const std::size_t np = (std::size_t)Nx * Ny;
+        std::vector<double> pos(3 * np), t0(np);
+        for (unsigned int ix = 0; ix < Nx; ix++)
+            for (unsigned int iy = 0; iy < Ny; iy++) {
+                const std::size_t p = (std::size_t)ix * Ny + iy;
+                Vector c = CellPosition(ix, iy);
+                pos[3 * p] = c.x;
+                pos[3 * p + 1] = c.y;
+                pos[3 * p + 2] = c.z;
+                t0[p] = CellTimeZero(ix, iy);
+            }
+        check_status(teufel_cuda_integrate_screen(source->device(), pos.data(), t0.data(), dt_obs,
+                                                  (int)NOTS, (int)np, buf.data(), nullptr),
+                     "ScreenObserver::integrate");
+    }
+
+    ElMagField getField(unsigned int ix, unsigned int iy, unsigned int it) const {
+        if (ix >= Nx || iy >= Ny || it >= NOTS)
+            throw IOexception("ScreenObserver::getField() - requested index out of range.");
+        ElMagField f;
+        std::memcpy(f.c, &buf[(((std::size_t)ix * Ny + iy) * NOTS + it) * 6], sizeof f.c);
+        return f;
+    }
+    std::size_t getBufferSize() override { return (std::size_t)Nx * Ny * NOTS * 6; }
+    double* getBuffer() override {
+        double* b = new double[getBufferSize()];
+        std::memcpy(b, buf.data(), sizeof(double) * getBufferSize());
+        return b;
+    }
+    void fromBuffer(double* buffer, std::size_t size) override {
+        if (size != getBufferSize())
+            throw IOexception("ScreenObserver::fromBuffer() - buffer size mismatch.");
+        std::memcpy(buf.data(), buffer, sizeof(double) * size);
+    }
+    void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
+
+private:
+    Vector Origin, dX, dY;
+    unsigned int Nx, Ny;
+    double t0_obs, dt_obs, dtx_obs, dty_obs;
+    unsigned int NOTS;
+    std::vector<double> buf;  // [Nx][Ny][NOTS][6]
+};
+
+// Observation points with individual trace start times (the integrate and
+// buffer part of MeshedScreen, src/mesh.cpp:289-316, 376-425).
+class MeshedScreen : public Observer<TrajectorySource> {
+public:
+    MeshedScreen(std::vector<Vector> points, std::vector<double> t0, double dt, int nt)
+        : pts(std::move(points)), T0(std::move(t0)), dt_obs(dt), Nt(nt),
+          buf(pts.size() * (std::size_t)nt * 6, 0.0) {
+        if (T0.size() != pts.size()) throw IOexception("MeshedScreen - t0 size mismatch.");
+    }
+    int get_Np() const { return (int)pts.size(); }
+    Vector get_point(int ip) const { return pts[ip]; }
+    double get_t0(int ip) const { return T0[ip]; }
+    void integrate() override {
+        if (!source) throw IOexception("MeshedScreen::integrate - no source set");
+        std::vector<double> pos(3 * pts.size());
+        for (std::size_t i = 0; i < pts.size(); i++) {
+            pos[3 * i] = pts[i].x;
+            pos[3 * i + 1] = pts[i].y;
+            pos[3 * i + 2] = pts[i].z;
+        }
+        check_status(teufel_cuda_integrate_screen(source->device(), pos.data(), T0.data(), dt_obs,
+                                                  Nt, (int)pts.size(), buf.data(), nullptr),
+                     "MeshedScreen::integrate");
+    }
+    std::size_t getBufferSize() override { return pts.size() * (std::size_t)Nt * 6; }
+    double* getBuffer() override {
+        double* b = new double[getBufferSize()];
+        std::memcpy(b, buf.data(), sizeof(double) * getBufferSize());
+        return b;
+    }
+    void fromBuffer(double* buffer, std::size_t size) override {
+        if (size != getBufferSize())
+            throw IOexception("MeshedScreen::fromBuffer() - buffer size mismatch.");
+        std::memcpy(buf.data(), buffer, sizeof(double) * size);
+    }
+    void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
+
+private:
+    std::vector<Vector> pts;
+    std::vector<double> T0;
+    double dt_obs;
+    int Nt;
+    std::vector<double> buf;  // [Np][Nt][6]
+};
+
+// One observation point (src/point_observer.cpp:30-110).
+class PointObserver : public Observer<TrajectorySource> {
+public:
+    PointObserver(Vector position, double t0, double dt, std::size_t nots)
+        : Pos(position), trace(t0, dt, nots) {}
+    void integrate() override {
+        if (!source) throw IOexception("PointObserver::integrate - no source set");
+        const double p[3] = {Pos.x, Pos.y, Pos.z};
+        check_status(teufel_cuda_integrate_point(source->device(), p, trace.get_t0(),
+                                                 trace.get_dt(), (int)trace.get_N(), trace.data(),
+                                                 nullptr),
+                     "PointObserver::integrate");
+    }
+    ElMagField getField(std::size_t it) const { return trace.get_field(it); }
+    std::size_t getBufferSize() override { return 6 * trace.get_N(); }
+    double* getBuffer() override {
+        double* b = new double[getBufferSize()];
+        if (getBufferSize()) std::memcpy(b, trace.data(), sizeof(double) * getBufferSize());
+        return b;
+    }
+    void fromBuffer(double* buffer, std::size_t size) override {
+        if (size != getBufferSize())
+            throw IOexception("PointObserver::fromBuffer() - buffer size mismatch.");
+        if (size) std::memcpy(trace.data(), buffer, sizeof(double) * size);
+    }
+
+private:
+    Vector Pos;
+    FieldTrace trace;
+};
+
+}  // namespace teufel_gb300

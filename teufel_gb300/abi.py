@@ -21,6 +21,8 @@ TEUFEL_ERR_CUDA = 3
 TEUFEL_ERR_RANGE = 4
 TEUFEL_ERR_NODEVICE = 6
 
+E_CHARGE = 1.6021766208e-19  # src/global.h:36
+
 PREC_FP32_SPLIT = 0
 PREC_FP64 = 1
 
@@ -138,7 +140,8 @@ class TrajSet:
         L = lib()
         n = traj.n_particles
         npnt = _c(traj.n_points, np.int32)
-        ch = _c(traj.charge)
+        # charge in Coulomb, formed as the reference forms Charge*ElementaryCharge
+        ch = _c(np.asarray(traj.charge, dtype=np.float64) * E_CHARGE)
         t, x, p, a = _c(traj.t), _c(traj.x), _c(traj.p), _c(traj.a)
         h = _vp()
         check(L.teufel_cuda_traj_upload(n, _ptr(npnt, _ip), _ptr(ch), _ptr(t), _ptr(x), _ptr(p),
@@ -149,7 +152,7 @@ class TrajSet:
 
     @classmethod
     def from_arrays(cls, n_points, charge, t, x, p, a):
-        """Upload from raw pointers-compatible arrays (host, possibly pinned)."""
+        """Upload from host arrays (possibly pinned); charge in units of e."""
         class _T:
             pass
         tr = _T()

@@ -296,9 +296,10 @@ struct BinSink {
 };
 
 // Scale of the Lienard-Wiechert field of one particle:
-// Charge*ElementaryCharge/(4.0*Pi*EpsNull), evaluated as src/particle.cpp:587.
-__device__ __forceinline__ double field_scale(double charge) {
-    return __ddiv_rn(__dmul_rn(charge, kE), __dmul_rn(__dmul_rn(4.0, kPi), kEps0));
+// Charge*ElementaryCharge/(4.0*Pi*EpsNull), evaluated as src/particle.cpp:587
+// from the charge in Coulomb (the product Charge*ElementaryCharge).
+__device__ __forceinline__ double field_scale(double charge_C) {
+    return __ddiv_rn(charge_C, __dmul_rn(__dmul_rn(4.0, kPi), kEps0));
 }
 
 __device__ __forceinline__ int warp_min(int v) { return __reduce_min_sync(0xffffffffu, v); }

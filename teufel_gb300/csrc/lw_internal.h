@@ -26,7 +26,7 @@ struct DevTraj {
     int64_t n_segments;         // total segments
     const int64_t* offsets;     // [n+1] first point of each particle
     const int64_t* seg_offsets; // [n+1] first segment of each particle
-    const double* charge;       // [n] units of e
+    const double* charge;       // [n] Coulomb
     const double4_32a* vhat;        // [n] frame direction of each particle (mean velocity), w = monotone flag
     const double4_32a* tx;          // [Npts] t, x, y, z                 (FP64, as uploaded)
     const double4_32a* pp;          // [Npts] beta*gamma, w unused        (FP64)

@@ -245,12 +245,12 @@ const char* teufel_cuda_status_string(int status) {
     }
 }
 
-int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* charge_e,
+int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* charge_C,
                             const double* t, const double* x, const double* bg, const double* a,
                             teufel_traj_set** out) {
     if (!out) return TEUFEL_ERR_ARG;
     *out = nullptr;
-    if (n_particles < 0 || (n_particles > 0 && (!n_points || !charge_e))) return TEUFEL_ERR_ARG;
+    if (n_particles < 0 || (n_particles > 0 && (!n_points || !charge_C))) return TEUFEL_ERR_ARG;
     int rc = check_device();
     if (rc) return rc;
     std::vector<int64_t> offs(n_particles + 1, 0), segs(n_particles + 1, 0);
@@ -262,7 +262,7 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     }
     const int64_t N = offs[n_particles];
     if (N > 0 && (!t || !x || !bg || !a)) return TEUFEL_ERR_ARG;
-    if (!finite_array(charge_e, n_particles)) return TEUFEL_ERR_ARG;
+    if (!finite_array(charge_C, n_particles)) return TEUFEL_ERR_ARG;
     teufel_traj_set* h = new (std::nothrow) teufel_traj_set();
     if (!h) return TEUFEL_ERR_NOMEM;
     h->h_seg_offsets = segs;
@@ -304,7 +304,7 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     if (cudaMemcpy(p_off, offs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
         cudaMemcpy(p_seg, segs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
         (n_particles > 0 &&
-         cudaMemcpy(p_charge, charge_e, sizeof(double) * n_particles, cudaMemcpyHostToDevice)) ||
+         cudaMemcpy(p_charge, charge_C, sizeof(double) * n_particles, cudaMemcpyHostToDevice)) ||
         cudaMemset(h->d_status, 0, sizeof(unsigned int)))
         return fail(cuda_fail(cudaGetLastError()));
     if (N > 0) {
