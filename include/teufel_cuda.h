@@ -117,6 +117,31 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set *traj, const double *p
                                     const double *pix_t0, double dt, int Nt, int Np, double *out,
                                     const teufel_options *opt, teufel_stream_t s);
 
+/* ---- allocation-free integration ---------------------------------------- */
+
+/* Size of the fixed device array the allocation-free entry point keeps its
+ * partial traces in (64 MiB, held by every GPU that loads the library). */
+#define TEUFEL_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+
+/* No counterpart in the reference (TEUFEL allocates its traces on the host).
+ * The FP32 split-precision integration of teufel_cuda_integrate_screen_ex for
+ * callers that cannot let the library call cudaMalloc: applications whose
+ * device memory belongs to another allocator, or that must not allocate once
+ * running because cudaMalloc/cudaFree can synchronize the device.  It makes no
+ * device allocation: the partial traces live in a fixed file-scope array of
+ * TEUFEL_NOALLOC_SCRATCH_BYTES.
+ *   d_pix_pos[Np][3], d_pix_t0[Np], d_out[Np][Nt][6]  device pointers; d_out is added into
+ * Limit: Np*Nt*6*sizeof(float) must not exceed TEUFEL_NOALLOC_SCRATCH_BYTES,
+ * otherwise TEUFEL_ERR_ARG is returned and nothing runs.  Larger observers
+ * run in several passes of as many slots as fit.  Synchronous at return.
+ * The array is shared by all calls and keeps the last call's contents (each
+ * call clears what it uses first); calls that overlap on the GPU race.  The
+ * first call on a device looks the array's address up on that device, so it
+ * should come before any stream capture. */
+int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set *traj, const double *d_pix_pos,
+                                         const double *d_pix_t0, double dt, int Nt, int Np,
+                                         double *d_out, teufel_stream_t s);
+
 /* ---- diagnostics used by the parity tests and the benchmark -------------- */
 
 /* Per trajectory point of particle m, as observed from pos with a trace

@@ -32,7 +32,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_LIB = LIBDIR / "libteufel_gb300.so"
 HARNESS_LIB = LIBDIR / "libteufel_harness.so"
 
-CU_SOURCES = ["teufel_abi.cu", "lw_fp64.cu", "lw_fp32.cu", "lw_support.cu"]
+CU_SOURCES = ["teufel_abi.cu", "lw_fp64.cu", "lw_fp32.cu", "lw_support.cu", "lw_noalloc.cu"]
 CU_HEADERS = ["lw_common.cuh", "lw_internal.h"]
 
 

@@ -32,8 +32,11 @@ EXPORTED = [
     "teufel_cuda_traj_free", "teufel_cuda_traj_points", "teufel_cuda_integrate_screen",
     "teufel_cuda_integrate_point", "teufel_cuda_integrate_screen_ex",
     "teufel_cuda_point_decisions", "teufel_cuda_deposit_injected", "teufel_cuda_last_inwindow",
-    "teufel_cuda_probe_peaks", "teufel_cuda_last_timing",
+    "teufel_cuda_probe_peaks", "teufel_cuda_last_timing", "teufel_cuda_integrate_screen_noalloc",
 ]
+
+# bytes of the fixed device array used by teufel_cuda_integrate_screen_noalloc
+NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 
 class Options(ctypes.Structure):
@@ -98,6 +101,9 @@ def lib():
         L.teufel_cuda_last_inwindow.argtypes = [_vp, _lp, _lp]
         L.teufel_cuda_last_timing.restype = ctypes.c_int
         L.teufel_cuda_last_timing.argtypes = [_vp, _lp, _ip, _dp, _dp]
+        L.teufel_cuda_integrate_screen_noalloc.restype = ctypes.c_int
+        L.teufel_cuda_integrate_screen_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_double,
+                                                           ctypes.c_int, ctypes.c_int, _vp, _vp]
         L.teufel_cuda_probe_peaks.restype = ctypes.c_int
         L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp]
         _lib = L

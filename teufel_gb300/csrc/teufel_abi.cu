@@ -222,6 +222,14 @@ bool valid_screen_args(const teufel_traj_set* traj, const double* pos, const dou
 
 }  // namespace
 
+namespace teufel {
+// device view and status word of a handle, for the allocation-free entry point
+const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** status) {
+    if (status) *status = traj->d_status;
+    return &traj->dev;
+}
+}  // namespace teufel
+
 extern "C" {
 
 void teufel_cuda_default_options(teufel_options* opt) {
