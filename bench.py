@@ -53,6 +53,8 @@ def parse():
                     help="integrate an evenly spaced subset of about this many pixels (0 = all)")
     ap.add_argument("--slots", type=int, default=0,
                     help="particle-range slots per launch (0 = library default)")
+    ap.add_argument("--nots", type=int, default=0,
+                    help="trace samples (0 = the workload's 4096); only for small profiling runs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -139,9 +141,8 @@ def make_batches(n_batches, batch, nthreads=0):
 
 
 def shard(n, rank, world):
-    lo = n * rank // world
-    hi = n * (rank + 1) // world
-    return lo, hi
+    from teufel_gb300.sharding import shard as _shard
+    return _shard(n, rank, world)
 
 
 # ---------------------------------------------------------------------------
@@ -240,7 +241,7 @@ def run_gb300(args):
     npts = int(w0.traj.n_points[0])
     lo, hi = shard(w0.n_pix, rank, world)
     n_pix = hi - lo
-    nots = w0.nots
+    nots = args.nots or w0.nots
     pos = torch.from_numpy(np.ascontiguousarray(w0.pix_pos[lo:hi])).to(dev)
     t0 = torch.from_numpy(np.ascontiguousarray(w0.pix_t0[lo:hi])).to(dev)
     out = torch.zeros((n_pix, nots, 6), dtype=torch.float64, device=dev)
@@ -252,7 +253,8 @@ def run_gb300(args):
                                                     n_pix, out.data_ptr(), stream=sptr,
                                                     timing=timing, n_slots=args.slots)
 
-    peak32, peak64 = abi.probe_peaks()
+    peak32, peak32x2, peak64 = abi.probe_peaks()
+    peak_fp32 = max(peak32, peak32x2)
     for j in range(W):
         step(j, False)
     barrier_sync()
@@ -364,12 +366,14 @@ def run_gb300(args):
                          "speedup_fp32_split_over_fp64": fp32_rate_sub / fp64_rate},
             "accuracy": {"rel_l2_fp32_split_vs_fp64": rel, "peak_sample_rel_err": peak_err,
                          "sample": f"{len(sub)} pixels x {args.batch} particles"},
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32,
-                         "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
+                         "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": TRAFFIC_PER_LAUNCH,
-                         "kernel": "lw_fp32_kernel",
-                         "peak_source": "FFMA throughput probe run by bench.py on this GPU "
+                         "kernel": "lw_fp32_uniform_kernel",
+                         "peak_source": "the larger of the FFMA and packed-FFMA2 throughput "
+                                        "probes run by bench.py on this GPU "
                                         "(MEASURED_PEAKS.json has no FP32 figure)",
+                         "ffma_probe_tflops": peak32, "ffma2_probe_tflops": peak32x2,
                          "algorithmic_flops": flops, "kernel_ms": kernel_ms,
                          "reduce_ms": reduce_ms, "fp64_probe_tflops": peak64},
             "gpu_launches": launches,

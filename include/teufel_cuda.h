@@ -62,7 +62,8 @@ typedef struct teufel_options {
     int precision;        /* TEUFEL_PREC_*                                        */
     int device_pointers;  /* 1: pix_pos, pix_t0 and out are device pointers      */
     int n_slots;          /* particle-range slots reduced in FP64; 0 = automatic  */
-    int threads_per_block;/* 0 = automatic (128)                                 */
+    int kernel_variant;   /* FP32 path: 0 = automatic, 1 = block-uniform steps,
+                             2 = per-pixel steps                                 */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
 } teufel_options;
@@ -151,7 +152,8 @@ int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set *traj, const doub
  * the FP32-path estimate of (ts-t0)/dt.  The same device functions as the
  * main FP32 kernel are used.  Arrays have n_points[m] entries (host memory). */
 int teufel_cuda_point_decisions(const teufel_traj_set *traj, int m, const double *pos, double t0,
-                                double dt, int Nt, int64_t *idx, int *flags, double *u_est);
+                                double dt, int Nt, int64_t *idx, int *flags, double *u_est,
+                                float *band);
 
 /* Run the device deposit routine on injected arrival times and fields (the
  * reference's known-answer test, tests/teufel.integrate_field.cpp:51-78,
@@ -176,9 +178,10 @@ int teufel_cuda_last_inwindow(const teufel_traj_set *traj, int64_t *inwindow,
 int teufel_cuda_last_timing(const teufel_traj_set *traj, int64_t *deposits, int *launches,
                             double *kernel_ms, double *reduce_ms);
 
-/* Peak FP32 FMA throughput of the current device measured with a dependent-
- * free FFMA kernel (TFLOP/s, FMA = 2 flops), and the same for FP64 DFMA. */
-int teufel_cuda_probe_peaks(double *fp32_tflops, double *fp64_tflops);
+/* Peak FMA throughput of the current device (TFLOP/s, FMA = 2 flops), each
+ * measured with independent FMA chains: scalar FP32 (FFMA), packed two-wide
+ * FP32 (fma.rn.f32x2) and FP64 (DFMA).  Any pointer may be NULL. */
+int teufel_cuda_probe_peaks(double *fp32_tflops, double *fp32x2_tflops, double *fp64_tflops);
 
 #ifdef __cplusplus
 }

@@ -41,7 +41,7 @@ NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device_pointers", ctypes.c_int),
-                ("n_slots", ctypes.c_int), ("threads_per_block", ctypes.c_int),
+                ("n_slots", ctypes.c_int), ("kernel_variant", ctypes.c_int),
                 ("timing", ctypes.c_int)]
 
 
@@ -92,7 +92,8 @@ def lib():
                                                       ctypes.POINTER(Options), _vp]
         L.teufel_cuda_point_decisions.restype = ctypes.c_int
         L.teufel_cuda_point_decisions.argtypes = [_vp, ctypes.c_int, _dp, ctypes.c_double,
-                                                  ctypes.c_double, ctypes.c_int, _lp, _ip, _dp]
+                                                  ctypes.c_double, ctypes.c_int, _lp, _ip, _dp,
+                                                  ctypes.POINTER(ctypes.c_float)]
         L.teufel_cuda_deposit_injected.restype = ctypes.c_int
         L.teufel_cuda_deposit_injected.argtypes = [ctypes.c_int, _ip, _dp, _dp, ctypes.c_double,
                                                    ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -105,7 +106,7 @@ def lib():
         L.teufel_cuda_integrate_screen_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_double,
                                                            ctypes.c_int, ctypes.c_int, _vp, _vp]
         L.teufel_cuda_probe_peaks.restype = ctypes.c_int
-        L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp]
+        L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -129,13 +130,14 @@ def _ptr(a, t=_dp):
 
 
 def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
-            n_slots: int = 0, timing: bool = False) -> Options:
+            n_slots: int = 0, timing: bool = False, variant: int = 0) -> Options:
     o = Options()
     lib().teufel_cuda_default_options(ctypes.byref(o))
     o.precision = precision
     o.device_pointers = 1 if device_pointers else 0
     o.n_slots = n_slots
     o.timing = 1 if timing else 0
+    o.kernel_variant = variant
     return o
 
 
@@ -189,7 +191,7 @@ class TrajSet:
     # -- integration ----------------------------------------------------
     def integrate_screen(self, pix_pos, pix_t0, dt, nots, out=None,
                          precision: int = PREC_FP32_SPLIT, n_slots: int = 0,
-                         stream: int = 0) -> np.ndarray:
+                         stream: int = 0, variant: int = 0) -> np.ndarray:
         """Traces of all particles on the pixels, added into ``out``
         ([Np][nots][6] doubles, zeros if None) -- host buffers."""
         pix_pos = _c(pix_pos).reshape(-1, 3)
@@ -199,7 +201,7 @@ class TrajSet:
             out = np.zeros((n_pix, nots, 6))
         if not (out.dtype == np.float64 and out.flags.c_contiguous):
             raise ValueError("out must be a C-contiguous float64 array")
-        opt = options(precision, False, n_slots)
+        opt = options(precision, False, n_slots, variant=variant)
         check(lib().teufel_cuda_integrate_screen_ex(self.handle, pix_pos.ctypes.data,
                                                     pix_t0.ctypes.data, dt, nots, n_pix,
                                                     out.ctypes.data, ctypes.byref(opt),
@@ -209,9 +211,10 @@ class TrajSet:
 
     def integrate_screen_device(self, pos_ptr: int, t0_ptr: int, dt: float, nots: int,
                                 n_pix: int, out_ptr: int, precision: int = PREC_FP32_SPLIT,
-                                n_slots: int = 0, stream: int = 0, timing: bool = False) -> None:
+                                n_slots: int = 0, stream: int = 0, timing: bool = False,
+                                variant: int = 0) -> None:
         """Device-pointer variant; returns once the work is enqueued."""
-        opt = options(precision, True, n_slots, timing)
+        opt = options(precision, True, n_slots, timing, variant)
         check(lib().teufel_cuda_integrate_screen_ex(self.handle, _vp(pos_ptr), _vp(t0_ptr), dt,
                                                     nots, n_pix, _vp(out_ptr),
                                                     ctypes.byref(opt), _vp(stream)),
@@ -248,10 +251,13 @@ class TrajSet:
         idx = np.zeros(n, dtype=np.int64)
         flags = np.zeros(n, dtype=np.int32)
         u = np.zeros(n)
+        band = np.zeros(n, dtype=np.float32)
         pos = _c(pos).reshape(3)
         check(lib().teufel_cuda_point_decisions(self.handle, m, _ptr(pos), t0, dt, nots,
-                                                _ptr(idx, _lp), _ptr(flags, _ip), _ptr(u)),
+                                                _ptr(idx, _lp), _ptr(flags, _ip), _ptr(u),
+                                                _ptr(band, ctypes.POINTER(ctypes.c_float))),
               "teufel_cuda_point_decisions")
+        self.last_band = band
         return idx, flags, u
 
 
@@ -270,7 +276,10 @@ def deposit_injected(ts_list, f_list, t0, dt, nots, precision=PREC_FP64, trace=N
 
 
 def probe_peaks():
+    """(FFMA, packed FFMA2, DFMA) throughput of the current device in TFLOP/s."""
     a = ctypes.c_double(0)
     b = ctypes.c_double(0)
-    check(lib().teufel_cuda_probe_peaks(ctypes.byref(a), ctypes.byref(b)), "probe_peaks")
-    return a.value, b.value
+    c = ctypes.c_double(0)
+    check(lib().teufel_cuda_probe_peaks(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+          "probe_peaks")
+    return a.value, b.value, c.value

@@ -295,6 +295,55 @@ struct BinSink {
     }
 };
 
+// The FP32 partial-trace sink: as BinSink, but the read half of the
+// read-modify-write is issued when a bin is opened and consumed only when it
+// is closed, several steps later, so its memory latency overlaps the work of
+// those steps instead of stalling the warp at every bin change.
+struct PrefetchSink {
+    float a[6];
+    float2 o0, o1, o2;  // the partial trace's previous content of the open bin
+    int open;
+    int nt;
+    float* row;  // this pixel's partial trace, [nt][6]
+    unsigned int err;
+    unsigned long long n_add;
+    __device__ void init(float* r, int n) {
+        row = r;
+        nt = n;
+        open = -1;
+        err = 0;
+        n_add = 0;
+    }
+    __device__ __forceinline__ void add(int k, const float* f) {
+        if (k < 0 || k >= nt) {
+            err |= 1u << TEUFEL_ERR_RANGE;
+            return;
+        }
+        n_add++;
+        if (k == open) {
+#pragma unroll
+            for (int c = 0; c < 6; c++) a[c] += f[c];
+        } else {
+            flush();
+            open = k;
+            const float2* p = reinterpret_cast<const float2*>(row + (int64_t)k * 6);
+            o0 = p[0];
+            o1 = p[1];
+            o2 = p[2];
+#pragma unroll
+            for (int c = 0; c < 6; c++) a[c] = f[c];
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        if (open < 0) return;
+        float2* p = reinterpret_cast<float2*>(row + (int64_t)open * 6);
+        p[0] = make_float2(o0.x + a[0], o0.y + a[1]);
+        p[1] = make_float2(o1.x + a[2], o1.y + a[3]);
+        p[2] = make_float2(o2.x + a[4], o2.y + a[5]);
+        open = -1;
+    }
+};
+
 // Scale of the Lienard-Wiechert field of one particle:
 // Charge*ElementaryCharge/(4.0*Pi*EpsNull), evaluated as src/particle.cpp:587
 // from the charge in Coulomb (the product Charge*ElementaryCharge).

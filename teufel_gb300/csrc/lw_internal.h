@@ -62,7 +62,11 @@ struct DevWork {
 
 // Kernel launchers (defined in the .cu files)
 namespace teufel {
-cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
+// FP32 kernel variants: all pixels of a block walk the same steps (uniform),
+// or every pixel walks its own in-window steps (lanes).
+constexpr int kVariantUniform = 0;
+constexpr int kVariantLanes = 1;
+cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp64(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
                         cudaStream_t s);
@@ -72,7 +76,7 @@ cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* ou
                                cudaStream_t s);
 cudaError_t launch_point_decisions(const DevTraj& tr, int m, double3 pos, double t0, double dt,
                                    int nt, int64_t n_points, int64_t* idx, int* flags,
-                                   double* u_est, cudaStream_t s);
+                                   double* u_est, float* band, cudaStream_t s);
 cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const double* ts,
                                     const double* f, double t0, double dt, int nt, int precision,
                                     double* trace, unsigned int* status, cudaStream_t s);
@@ -81,5 +85,5 @@ cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const dou
                                       const double* f, double t0, double dt, int nt,
                                       double* trace, float* trace32, unsigned int* status,
                                       cudaStream_t s);
-int probe_peaks(double* fp32_tflops, double* fp64_tflops);
+int probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops);
 }  // namespace teufel

@@ -138,7 +138,7 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
         w.slot_stride = (int64_t)Np * Nt * 6;
         w.status = d_status;
         w.counters = nullptr;
-        e = launch_fp32(*tr, sc, w, kNoallocThreads, s);
+        e = launch_fp32(*tr, sc, w, kVariantUniform, s);
         if (!e) e = launch_reduce_fp32(w, sc, d_out, s);
         if (e) return fail(e);
     }

@@ -189,7 +189,10 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         w.counters = h->d_counters;
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used], s));
         cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
-                             : launch_fp32(h->dev, sc, w, kThreads, s);
+                             : launch_fp32(h->dev, sc, w,
+                                           opt.kernel_variant == 2 ? kVariantLanes
+                                                                   : kVariantUniform,
+                                           s);
         if (e != cudaSuccess) return cuda_fail(e);
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 1], s));
         e = fp64 ? launch_reduce_fp64(w, sc, d_out, s) : launch_reduce_fp32(w, sc, d_out, s);
@@ -237,7 +240,7 @@ void teufel_cuda_default_options(teufel_options* opt) {
     opt->precision = TEUFEL_PREC_FP32_SPLIT;
     opt->device_pointers = 0;
     opt->n_slots = 0;
-    opt->threads_per_block = 0;
+    opt->kernel_variant = 0;
     opt->timing = 0;
 }
 
@@ -460,7 +463,8 @@ int teufel_cuda_last_timing(const teufel_traj_set* traj, int64_t* deposits, int*
 }
 
 int teufel_cuda_point_decisions(const teufel_traj_set* traj, int m, const double* pos, double t0,
-                                double dt, int Nt, int64_t* idx, int* flags, double* u_est) {
+                                double dt, int Nt, int64_t* idx, int* flags, double* u_est,
+                                float* band) {
     if (!traj || !pos || !idx || !flags || !u_est || m < 0 || m >= traj->dev.n_particles ||
         Nt < 0 || !(dt != 0.0))
         return TEUFEL_ERR_ARG;
@@ -472,17 +476,21 @@ int teufel_cuda_point_decisions(const teufel_traj_set* traj, int m, const double
     int64_t* d_idx = nullptr;
     int* d_flags = nullptr;
     double* d_u = nullptr;
+    float* d_band = nullptr;
     TRY_CUDA(cudaMalloc(&d_idx, sizeof(int64_t) * n));
     TRY_CUDA(cudaMalloc(&d_flags, sizeof(int) * n));
     TRY_CUDA(cudaMalloc(&d_u, sizeof(double) * n));
+    TRY_CUDA(cudaMalloc(&d_band, sizeof(float) * n));
     cudaError_t e = launch_point_decisions(h->dev, m, make_double3(pos[0], pos[1], pos[2]), t0, dt,
-                                           Nt, n, d_idx, d_flags, d_u, 0);
+                                           Nt, n, d_idx, d_flags, d_u, d_band, 0);
     if (!e) e = cudaMemcpy(idx, d_idx, sizeof(int64_t) * n, cudaMemcpyDeviceToHost);
     if (!e) e = cudaMemcpy(flags, d_flags, sizeof(int) * n, cudaMemcpyDeviceToHost);
     if (!e) e = cudaMemcpy(u_est, d_u, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (!e && band) e = cudaMemcpy(band, d_band, sizeof(float) * n, cudaMemcpyDeviceToHost);
     cudaFree(d_idx);
     cudaFree(d_flags);
     cudaFree(d_u);
+    cudaFree(d_band);
     return e ? cuda_fail(e) : TEUFEL_OK;
 }
 
@@ -530,10 +538,10 @@ int teufel_cuda_deposit_injected(int n_particles, const int* n_points, const dou
     return status_from_mask(mask);
 }
 
-int teufel_cuda_probe_peaks(double* fp32_tflops, double* fp64_tflops) {
+int teufel_cuda_probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops) {
     int rc = check_device();
     if (rc) return rc;
-    return probe_peaks(fp32_tflops, fp64_tflops) ? TEUFEL_ERR_CUDA : TEUFEL_OK;
+    return probe_peaks(fp32_tflops, fp32x2_tflops, fp64_tflops) ? TEUFEL_ERR_CUDA : TEUFEL_OK;
 }
 
 }  // extern "C"
