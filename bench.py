@@ -369,7 +369,7 @@ def run_gb300(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": TRAFFIC_PER_LAUNCH,
-                         "kernel": "lw_fp32_uniform_kernel",
+                         "kernel": "lw_fp32_warp_kernel",
                          "peak_source": "the larger of the FFMA and packed-FFMA2 throughput "
                                         "probes run by bench.py on this GPU "
                                         "(MEASURED_PEAKS.json has no FP32 figure)",

@@ -1,6 +1,6 @@
 """In-tree build of the native libraries.
 
-Three shared objects are produced inside the package (``teufel_gb300/_lib``):
+Two shared objects are produced inside the package (``teufel_gb300/_lib``):
 
 * ``libteufel_gb300.so`` -- the CUDA field-integration kernels and the C-ABI
   declared in ``include/teufel_cuda.h`` (nvcc, sm_103a only);
@@ -32,8 +32,9 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_LIB = LIBDIR / "libteufel_gb300.so"
 HARNESS_LIB = LIBDIR / "libteufel_harness.so"
 
-CU_SOURCES = ["teufel_abi.cu", "lw_fp64.cu", "lw_fp32.cu", "lw_support.cu", "lw_noalloc.cu"]
-CU_HEADERS = ["lw_common.cuh", "lw_internal.h"]
+CU_SOURCES = ["teufel_abi.cu", "lw_fp64.cu", "lw_fp32_main.cu", "lw_fp32_warp.cu",
+              "lw_support.cu", "lw_noalloc.cu"]
+CU_HEADERS = ["lw_common.cuh", "lw_internal.h", "lw_fp32_point.cuh"]
 
 
 def _newer(out: Path, deps) -> bool:

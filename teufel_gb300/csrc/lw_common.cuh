@@ -104,8 +104,8 @@ __device__ __forceinline__ void inwindow_steps(const double4_32a* tx, int st_lo,
 }
 
 // ---------------------------------------------------------------------------
-// Arithmetic policies for the deposit: the FP64 path uses IEEE-rounded
-// operations in the reference's order, the FP32 path plain float operations.
+// Arithmetic policy of the generic deposit: IEEE-rounded FP64 operations in
+// the reference's order (the FP32 path has its own deposit_step32).
 // ---------------------------------------------------------------------------
 struct Ops64 {
     typedef double T;
@@ -114,17 +114,9 @@ struct Ops64 {
     __device__ static T mul(T a, T b) { return __dmul_rn(a, b); }
     __device__ static T div(T a, T b) { return __ddiv_rn(a, b); }
 };
-struct Ops32 {
-    typedef float T;
-    __device__ static T add(T a, T b) { return a + b; }
-    __device__ static T sub(T a, T b) { return a - b; }
-    __device__ static T mul(T a, T b) { return a * b; }
-    __device__ static T div(T a, T b) { return __fdividef(a, b); }
-};
-
 // Time coordinates of the bins.  Geo64 works in seconds exactly as the
 // reference (t_center = t0 + idx*dt etc., src/particle.cpp:812, 816, 845,
-// 851, 856); Geo32 works in bin units relative to an integer base B.
+// 851, 856).
 struct Geo64 {
     double t0, dt;
     __device__ double center(int k) const { return __dadd_rn(t0, __dmul_rn((double)k, dt)); }
@@ -136,14 +128,6 @@ struct Geo64 {
     }
     __device__ double per_dt(double x) const { return __ddiv_rn(x, dt); }
 };
-struct Geo32 {
-    long long B;
-    __device__ float center(int k) const { return (float)((long long)k - B); }
-    __device__ float start(int k) const { return (float)((long long)k - B) - 0.5f; }
-    __device__ float end(int k) const { return (float)((long long)k - B) + 0.5f; }
-    __device__ float per_dt(float x) const { return x; }
-};
-
 // One step of ChargedParticle::integrateFieldTrace (src/particle.cpp:786-865):
 // the linear interpolant of the field over [ts1, ts2] is averaged over every
 // bin it overlaps.  Decisions (window, case, indices) come from the point
@@ -291,55 +275,6 @@ struct BinSink {
     __device__ __forceinline__ void flush() {
         if (open < 0) return;
         add_row(row + (int64_t)open * STRIDE, a);
-        open = -1;
-    }
-};
-
-// The FP32 partial-trace sink: as BinSink, but the read half of the
-// read-modify-write is issued when a bin is opened and consumed only when it
-// is closed, several steps later, so its memory latency overlaps the work of
-// those steps instead of stalling the warp at every bin change.
-struct PrefetchSink {
-    float a[6];
-    float2 o0, o1, o2;  // the partial trace's previous content of the open bin
-    int open;
-    int nt;
-    float* row;  // this pixel's partial trace, [nt][6]
-    unsigned int err;
-    unsigned long long n_add;
-    __device__ void init(float* r, int n) {
-        row = r;
-        nt = n;
-        open = -1;
-        err = 0;
-        n_add = 0;
-    }
-    __device__ __forceinline__ void add(int k, const float* f) {
-        if (k < 0 || k >= nt) {
-            err |= 1u << TEUFEL_ERR_RANGE;
-            return;
-        }
-        n_add++;
-        if (k == open) {
-#pragma unroll
-            for (int c = 0; c < 6; c++) a[c] += f[c];
-        } else {
-            flush();
-            open = k;
-            const float2* p = reinterpret_cast<const float2*>(row + (int64_t)k * 6);
-            o0 = p[0];
-            o1 = p[1];
-            o2 = p[2];
-#pragma unroll
-            for (int c = 0; c < 6; c++) a[c] = f[c];
-        }
-    }
-    __device__ __forceinline__ void flush() {
-        if (open < 0) return;
-        float2* p = reinterpret_cast<float2*>(row + (int64_t)open * 6);
-        p[0] = make_float2(o0.x + a[0], o0.y + a[1]);
-        p[1] = make_float2(o1.x + a[2], o1.y + a[3]);
-        p[2] = make_float2(o2.x + a[4], o2.y + a[5]);
         open = -1;
     }
 };

@@ -1,0 +1,405 @@
+// lw_fp32_point.cuh -- device functions of the split-precision path shared by
+// its kernels (lw_fp32_main.cu, lw_fp32_warp.cu): the per-pixel double-float
+// constants, the FP64 segment anchors, the FP32 field of one trajectory point,
+// the compensated FP32 arrival chain with its error bound, the exact-fallback
+// decision and the deposit of one step in bin units.  The derivations are in
+// the header comment of lw_fp32_main.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lw_common.cuh"
+
+namespace teufel {
+
+// ---------------------------------------------------------------------------
+// Double-float helpers (error-free transformations)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+    s = a + b;
+    double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void two_prod(double a, double b, double& p, double& e) {
+    p = a * b;
+    e = fma(a, b, -p);
+}
+
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs: one add.f32x2 / mul.f32x2 / fma.f32x2 instruction does
+// two IEEE round-to-nearest single-precision operations.
+// ---------------------------------------------------------------------------
+union F2U {
+    float2 f;
+    unsigned long long u;
+};
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    F2U x, y, r;
+    x.f = a;
+    y.f = b;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(x.u), "l"(y.u));
+    return r.f;
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return add2(a, make_float2(-b.x, -b.y));
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    F2U x, y, r;
+    x.f = a;
+    y.f = b;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(x.u), "l"(y.u));
+    return r.f;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    F2U x, y, z, r;
+    x.f = a;
+    y.f = b;
+    z.f = c;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.u) : "l"(x.u), "l"(y.u), "l"(z.u));
+    return r.f;
+}
+
+// ---------------------------------------------------------------------------
+// Pixel, anchor and point evaluation (shared by the main kernel and the
+// decision record used by the bin-index parity tests)
+// ---------------------------------------------------------------------------
+struct PixelCtx {
+    double3 P;
+    double3 Ph;   // P / |P|
+    double Pn;    // |P|
+    double Tp;    // |P|/c - t0, formed in double-float
+    Window w;
+    double inv_dt;
+    float kdt;    // 1/dt
+    float refb0;  // the reference's rounding of t0 and of the flight time [bins]
+};
+
+__device__ __forceinline__ PixelCtx make_pixel(double3 P, double t0, double dt, int nt) {
+    PixelCtx c;
+    c.P = P;
+    c.w = make_window(t0, dt, nt);
+    c.inv_dt = 1.0 / dt;
+    c.kdt = (float)c.inv_dt;
+    // |P|^2 and |P| in double-float
+    double s, e, p, q, e2;
+    two_prod(P.x, P.x, s, e);
+    two_prod(P.y, P.y, p, q);
+    two_sum(s, p, s, e2);
+    e += q + e2;
+    two_prod(P.z, P.z, p, q);
+    two_sum(s, p, s, e2);
+    e += q + e2;
+    double n_hi = sqrt(s);
+    double n_lo = n_hi > 0.0 ? (fma(-n_hi, n_hi, s) + e) / (2.0 * n_hi) : 0.0;
+    c.Pn = n_hi;
+    double r = n_hi > 0.0 ? 1.0 / n_hi : 0.0;
+    c.Ph = make_double3(P.x * r, P.y * r, P.z * r);
+    // |P|/c - t0 with 1/c as a double-float
+    const double ic_hi = 1.0 / kC;
+    const double ic_lo = fma(-ic_hi, kC, 1.0) / kC;
+    double qh, ql;
+    two_prod(n_hi, ic_hi, qh, ql);
+    ql += n_hi * ic_lo + n_lo * ic_hi;
+    double d, de;
+    two_sum(qh, -t0, d, de);
+    c.Tp = d + (de + ql);
+    // the reference rounds |P - x|/c (~ |P|/c) and t + R/c; t0 and tmin/tmax
+    c.refb0 = (float)((n_hi / kC * 4.5e-16 + fabs(t0) * 2.3e-16) * c.inv_dt);
+    return c;
+}
+
+// Arrival coordinates are held relative to the current anchor's integer bin
+// B as (ki, r): (ts - t0)/dt = B + ki + r, |r| <= 1/2 normally.  B is kept
+// within +-2^29 so that B + ki never overflows 32 bits; anchors farther out
+// than that send every point of their segment through the exact path.
+constexpr double kBinLimit = 536870912.0;  // 2^29
+
+struct Anchor {
+    long long B;   // floor of the anchor's (ts - t0)/dt, clamped to +-2^29
+    int Bi;        // the same, as int
+    float frac;    // the rest, in [0, 1)
+    float Dx, Dy, Dz;
+    float err;     // bound on the anchor's error plus the reference's rounding [bins]
+};
+
+__device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const PixelCtx& px) {
+    const double Dx = px.P.x - a.y, Dy = px.P.y - a.z, Dz = px.P.z - a.w;
+    const double pa = fma(px.Ph.x, a.y, fma(px.Ph.y, a.z, px.Ph.z * a.w));  // P^.x
+    const double L = px.Pn - pa;
+    const double cx = a.z * px.Ph.z - a.w * px.Ph.y;
+    const double cy = a.w * px.Ph.x - a.y * px.Ph.z;
+    const double cz = a.y * px.Ph.y - a.z * px.Ph.x;
+    const double g2 = fma(cx, cx, fma(cy, cy, cz * cz));  // |x x P^|^2
+    double G;
+    if (L > 0.0 && g2 < 1.0e-4 * L * L) {
+        // G = g2 / (L + sqrt(L^2 + g2)) as a series in q = g2/L^2
+        double rL = (double)__frcp_rn((float)L);
+        rL = rL * fma(-L, rL, 2.0);
+        rL = rL * fma(-L, rL, 2.0);
+        const double q = g2 * rL * rL;
+        G = g2 * rL * fma(q, fma(q, 0.0625, -0.125), 0.5);
+    } else {
+        G = g2 / (L + sqrt(fma(L, L, g2)));
+    }
+    const double ic = 1.0 / kC;
+    const double tau = fma(-pa, ic, a.x);  // t - P^.x / c
+    const double u0 = (px.Tp + tau + G * ic) * px.inv_dt;
+    const double u = fmax(-kBinLimit, fmin(u0, kBinLimit));
+    const double fl = floor(u);
+    A.B = (long long)fl;
+    A.Bi = (int)fl;
+    A.frac = (float)(u - fl);
+    A.Dx = (float)Dx;
+    A.Dy = (float)Dy;
+    A.Dz = (float)Dz;
+    // our rounding: t, P^.x/c and their sum, G/c, the sum with Tp, the scaling
+    const float own = (float)((fabs(a.x) + fabs(pa) * ic + fabs(px.Tp) + G * ic) * px.inv_dt *
+                              4.5e-16) +
+                      (float)(fabs(u) * 4.5e-16) + 1.0e-7f;
+    A.err = own + px.refb0 + (float)(fabs(a.x) * px.inv_dt * 4.5e-16);
+    if (u != u0) A.err = 1.0f;  // clamped: resolve the segment exactly
+}
+
+struct PointState {
+    int ki;        // integer part of (ts - t0)/dt - B
+    float r;       // the rest
+    int idx;       // bin index round((ts-t0)/dt), clamped to [-2, nt+1]
+    int flags;     // kLeTmin | kLtTmax | kExact
+    float dt;      // duration of the trajectory step that starts at this point
+    float Nx, Ny, Nz;
+    float2 f[3];   // (Ex, Ey), (Ez, c*Bx), (c*By, c*Bz): packed for the f32x2 pipe
+};
+
+// Field of one point from its anchor-relative position.
+__device__ __forceinline__ void point_field(PointState& S, float4 a, float4 b, float4 c,
+                                            const Anchor& A) {
+    const float Dx = A.Dx - a.x, Dy = A.Dy - a.y, Dz = A.Dz - a.z;
+    const float R2 = Dx * Dx + Dy * Dy + Dz * Dz;
+    const float iR = rsqrtf(R2);
+    const float Nx = Dx * iR, Ny = Dy * iR, Nz = Dz * iR;
+    S.Nx = Nx;
+    S.Ny = Ny;
+    S.Nz = Nz;
+    S.dt = a.w;
+    // kappa = 1 - n.beta in split form
+    const float Wx = b.y * Nz - b.z * Ny, Wy = b.z * Nx - b.x * Nz, Wz = b.x * Ny - b.y * Nx;
+    const float s2 = Wx * Wx + Wy * Wy + Wz * Wz;
+    const float rc1 = __fdividef(1.0f, 1.0f + (b.x * Nx + b.y * Ny + b.z * Nz));
+    const float kappa = b.w + (1.0f - b.w) * s2 * rc1;
+    // N - beta = W x (N + beta_hat) / c1 + beta_hat * eps
+    const float Sx = Nx + b.x, Sy = Ny + b.y, Sz = Nz + b.z;
+    const float mbx = (Wy * Sz - Wz * Sy) * rc1 + b.x * b.w;
+    const float mby = (Wz * Sx - Wx * Sz) * rc1 + b.y * b.w;
+    const float mbz = (Wx * Sy - Wy * Sx) * rc1 + b.z * b.w;
+    const float rk = __fdividef(1.0f, kappa);
+    const float irk2 = iR * rk * rk;
+    const float cacc = irk2 * rk;   // 1/(R kappa^3), times scale/c folded into beta'
+    const float cvel = c.w * iR * cacc;
+    // N x ((N - beta) x beta') = (N - beta)(N.beta') - beta' (N.(N - beta)) with
+    // N.(N - beta) = kappa, so E = (N - beta) s1 - beta' s2
+    const float nbp = Nx * c.x + Ny * c.y + Nz * c.z;
+    const float su = fmaf(cacc, nbp, cvel);
+    const float sb = irk2;  // cacc * kappa
+    const float Ex = mbx * su - c.x * sb;
+    const float Ey = mby * su - c.y * sb;
+    const float Ez = mbz * su - c.z * sb;
+    S.f[0] = make_float2(Ex, Ey);
+    S.f[1] = make_float2(Ez, Ny * Ez - Nz * Ey);
+    S.f[2] = make_float2(Nz * Ex - Nx * Ez, Nx * Ey - Ny * Ex);
+}
+
+// Arrival increment of the step from point 1 to point 2 [bins]:
+//   dt (1 - |beta_c| + |beta_c| (1 - |n_m|) + |beta_c| |n_m| (1 - cos theta))
+// with n_m along N1 + N2, 1 - |n_m| = |N1 - N2|^2 / 8 to leading order, and
+// 1 - cos theta = |beta_c x s|^2 / (|s| (|s| + beta_c.s)), s = N1 + N2, |s| ~ 2
+// (|s| = 2 - |N1 - N2|^2/4, and the FP32 normalisation of N is good to 1e-7).
+__device__ __forceinline__ float step_increment(const PointState& p1, const PointState& p2,
+                                                float4 chord, float kdt) {
+    const float sx = p1.Nx + p2.Nx, sy = p1.Ny + p2.Ny, sz = p1.Nz + p2.Nz;
+    const float dx = p1.Nx - p2.Nx, dy = p1.Ny - p2.Ny, dz = p1.Nz - p2.Nz;
+    const float wx = chord.y * sz - chord.z * sy;
+    const float wy = chord.z * sx - chord.x * sz;
+    const float wz = chord.x * sy - chord.y * sx;
+    const float w2 = wx * wx + wy * wy + wz * wz;
+    const float bs = chord.x * sx + chord.y * sy + chord.z * sz;
+    const float one_m_cos = __fdividef(w2, 4.0f + 2.0f * bs);
+    const float one_m_n = 0.125f * (dx * dx + dy * dy + dz * dz);
+    const float kap = chord.w + (1.0f - chord.w) * (one_m_n + one_m_cos);
+    return p1.dt * kdt * kap;
+}
+
+// Advance the compensated arrival chain from p1 to p2 by du.
+__device__ __forceinline__ void chain_step(const PointState& p1, PointState& p2, float du,
+                                           float& comp) {
+    const float y = du - comp;
+    float t = p1.r + y;
+    comp = (t - p1.r) - y;
+    t = fminf(fmaxf(t, -4.0e8f), 4.0e8f);
+    const float k = rintf(t);
+    p2.r = t - k;
+    p2.ki = p1.ki + (int)k;
+}
+
+// Bin decision from (ki, r); falls back to the reference's exact FP64
+// evaluation when r is within `band` of +-1/2.
+__device__ __forceinline__ bool decide(PointState& S, float band, const double4_32a* tx,
+                                       int64_t i, const PixelCtx& px, const Anchor& A) {
+    const float d = 0.5f - fabsf(S.r);  // distance to the nearest half-integer
+    if (d <= band) {
+        const double ts = exact_retarded_time(tx[i], px.P);
+        S.idx = exact_bin(ts, px.w);
+        S.flags = exact_flags(ts, px.w);
+        // continue from the exact value
+        double v = (ts - px.w.t0) * px.inv_dt - (double)A.B;
+        v = fmax(-kBinLimit, fmin(v, kBinLimit));
+        const double k = floor(v + 0.5);
+        S.ki = (int)k;
+        S.r = (float)(v - k);
+        return true;
+    }
+    int k = A.Bi + S.ki;
+    const int nt = px.w.nt;
+    k = k < -2 ? -2 : (k > nt + 1 ? nt + 1 : k);
+    S.idx = k;
+    S.flags = (k < 0 ? kLeTmin : 0) | (k < nt ? kLtTmax : 0);
+    return false;
+}
+
+// Start a compensated arrival chain at an anchor point.
+__device__ __forceinline__ void start_chain(PointState& S, const Anchor& A) {
+    const float k = rintf(A.frac);  // 0 or 1
+    S.ki = (int)k;
+    S.r = A.frac - k;
+}
+
+// Re-express a point against a new anchor.
+__device__ __forceinline__ void rebase(PointState& S, const Anchor& from, const Anchor& to) {
+    S.ki += (int)(from.B - to.B);
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 partial-trace sink.  Contributions to the same bin are summed in
+// registers; the read half of the bin's read-modify-write is issued when the
+// bin is opened and consumed only when it is closed, several steps later, so
+// its memory latency overlaps the work of those steps instead of stalling the
+// warp at every bin change.  All arithmetic is on packed pairs.
+// ---------------------------------------------------------------------------
+struct PrefetchSink {
+    float2 a[3];
+    float2 o[3];  // the partial trace's previous content of the open bin
+    int open;
+    int nt;
+    float* row;  // this pixel's partial trace, [nt][6]
+    unsigned int err;
+    unsigned long long n_add;
+    __device__ void init(float* r, int n) {
+        row = r;
+        nt = n;
+        open = -1;
+        err = 0;
+        n_add = 0;
+    }
+    __device__ __forceinline__ void add(int k, const float2* f) {
+        if (k < 0 || k >= nt) {
+            err |= 1u << TEUFEL_ERR_RANGE;
+            return;
+        }
+        n_add++;
+        if (k == open) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) a[c] = add2(a[c], f[c]);
+        } else {
+            flush();
+            open = k;
+            const float2* p = reinterpret_cast<const float2*>(row + (int64_t)k * 6);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                o[c] = p[c];
+                a[c] = f[c];
+            }
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        if (open < 0) return;
+        float2* p = reinterpret_cast<float2*>(row + (int64_t)open * 6);
+#pragma unroll
+        for (int c = 0; c < 3; c++) p[c] = add2(o[c], a[c]);
+        open = -1;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// The deposit of one step in bin units from (ki, r) coordinates on base Bi;
+// the same branch structure and weights as deposit_step (lw_common.cuh),
+// src/particle.cpp:786-865.
+// ---------------------------------------------------------------------------
+template <class Sink>
+__device__ __forceinline__ bool deposit_step32(const PointState& p1, const PointState& p2, int Bi,
+                                               int nt, Sink& sink) {
+    if ((p2.flags & kLeTmin) || !(p1.flags & kLtTmax)) return false;
+    const float dts = (float)(p2.ki - p1.ki) + (p2.r - p1.r);
+    float2 field[3];
+    const int idx2 = p2.idx > nt ? nt : p2.idx;
+    const int u1i = Bi + p1.ki, u2i = Bi + p2.ki;  // integer parts of u1, u2
+    const float rd = __fdividef(1.0f, dts);
+    if (!(p1.flags & kLeTmin) && idx2 - p1.idx <= 1) {
+        // The common case, without branches: the step lies in bin idx1 or
+        // crosses its upper edge e = idx1 + 1/2 into idx2 = idx1 + 1.  With
+        // e' = min(u2, e) and f(e') the interpolant there, bin idx1 receives
+        // (e' - u1)(f1 + f(e'))/2 and bin idx2 (u2 - e')(f(e') + f2)/2 -- the
+        // single-bin weight (f1 + f2)/2 dts, and the first and last partial
+        // bins of the reference (src/particle.cpp:835-862), in one form.
+        const bool split = idx2 > p1.idx;
+        const float a = split ? (float)(p1.idx - u1i) + 0.5f - p1.r : dts;  // e' - u1
+        const float2 lam = splat2(a * rd);
+        float2 fe[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) fe[c] = fma2(sub2(p2.f[c], p1.f[c]), lam, p1.f[c]);
+        const float2 w1 = splat2(0.5f * a);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = mul2(add2(p1.f[c], fe[c]), w1);
+        sink.add(p1.idx, field);
+        if (split && idx2 < nt) {
+            const float2 w2 = splat2(0.5f * (dts - a));
+#pragma unroll
+            for (int c = 0; c < 3; c++) field[c] = mul2(add2(fe[c], p2.f[c]), w2);
+            sink.add(idx2, field);
+        }
+        return true;
+    }
+    int kfull0;
+    if (p1.flags & kLeTmin) {
+        kfull0 = 0;
+    } else {
+        // first partial bin idx1
+        const int idx1 = p1.idx;
+        const float b2 = (float)(u2i - idx1) - 0.5f + p2.r;  // ts2 - t_end
+        const float b1 = (float)(idx1 - u1i) + 0.5f - p1.r;  // t_end - ts1
+        const float2 w1 = splat2(1.0f + b2 * rd), w2 = splat2(b1 * rd), wb = splat2(0.5f * b1);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = mul2(fma2(p1.f[c], w1, mul2(p2.f[c], w2)), wb);
+        sink.add(idx1, field);
+        kfull0 = idx1 + 1;
+    }
+    for (int k = kfull0; k < idx2; k++) {
+        const float2 w1 = splat2(((float)(u2i - k) + p2.r) * rd);
+        const float2 w2 = splat2(((float)(k - u1i) - p1.r) * rd);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = fma2(p1.f[c], w1, mul2(p2.f[c], w2));
+        sink.add(k, field);
+    }
+    if (idx2 < nt) {
+        const float a2 = (float)(u2i - idx2) + p2.r + 0.5f;  // ts2 - t_start
+        const float a1 = (float)(idx2 - u1i) - 0.5f - p1.r;  // t_start - ts1
+        const float2 w1 = splat2(a2 * rd), w2 = splat2(1.0f + a1 * rd), wb = splat2(0.5f * a2);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = mul2(fma2(p1.f[c], w1, mul2(p2.f[c], w2)), wb);
+        sink.add(idx2, field);
+    }
+    return true;
+}
+
+constexpr float kChainRel = 1.0e-6f;  // bound on the relative error of one FP32 increment
+
+}  // namespace teufel

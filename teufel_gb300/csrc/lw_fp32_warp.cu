@@ -1,0 +1,151 @@
+// lw_fp32_warp.cu -- the warp-uniform split-precision kernel (the default).
+//
+// Each warp owns 32 pixels and works on its own: for every particle of its
+// slot it walks the union of its lanes' in-window step ranges, all 32 lanes on
+// the same trajectory point at the same time.  The particle's per-point data
+// (64 B per point) is staged into the warp's own shared-memory double buffer,
+// one segment (kSegLen points) at a time, with cp.async; every lane then reads
+// it as a broadcast.  No block-wide barrier is involved, so warps never wait
+// for one another, and a warp's step range is only as wide as its own 32
+// pixels need.  The per-point work is in lw_fp32_point.cuh.
+#include <cuda_runtime.h>
+
+#include "lw_fp32_point.cuh"
+
+namespace teufel {
+
+constexpr int kWThreads = 256;
+constexpr int kWWarps = kWThreads / 32;
+
+struct __align__(16) WarpChunk {
+    float4 q0[kSegLen], q1[kSegLen], q2[kSegLen], q3[kSegLen];
+};
+
+// The 32 lanes copy the four per-point arrays of `avail` points starting at p0.
+__device__ __forceinline__ void warp_stage(WarpChunk* b, const DevTraj& tr, int64_t p0, int avail,
+                                           int lane) {
+#pragma unroll
+    for (int k = 0; k < 4 * kSegLen / 32; k++) {
+        const int t = lane + 32 * k;
+        const int arr = t / kSegLen, l = t % kSegLen;
+        if (l < avail) {
+            const float4* src = arr == 0 ? tr.q0 : arr == 1 ? tr.q1 : arr == 2 ? tr.q2 : tr.q3;
+            float4* dst = arr == 0 ? b->q0 : arr == 1 ? b->q1 : arr == 2 ? b->q2 : b->q3;
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + l);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+                         "l"(src + p0 + l)
+                         : "memory");
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kWThreads, 2)
+    lw_fp32_warp_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
+    __shared__ WarpChunk buf[kWWarps][2];
+    // the FP64 pixel constants are needed only at anchors and in the exact
+    // fallback: kept in shared memory rather than in registers
+    __shared__ PixelCtx pxs[kWThreads];
+    const int slot = blockIdx.y;
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool active = pix < sc.np;
+    const int pc = active ? pix : sc.np - 1;
+    const double3 P = make_double3(sc.pix_pos[3 * pc], sc.pix_pos[3 * pc + 1],
+                                   sc.pix_pos[3 * pc + 2]);
+    pxs[threadIdx.x] = make_pixel(P, sc.pix_t0[pc], sc.dt, sc.nt);
+    const PixelCtx& px = pxs[threadIdx.x];
+    WarpChunk* wb = buf[warp];
+    PrefetchSink sink;
+    sink.init(static_cast<float*>(wk.scratch) + (int64_t)slot * wk.slot_stride +
+                  (int64_t)pc * sc.nt * 6,
+              sc.nt);
+    const int64_t g0 = wk.slot_seg[slot], g1 = wk.slot_seg[slot + 1];
+    int m = g0 < g1 ? particle_of_segment(tr.seg_offsets, tr.n_particles, g0) : tr.n_particles;
+    unsigned long long inwin = 0, nfb = 0;
+    for (; m < tr.n_particles && tr.seg_offsets[m] < g1; ++m) {
+        const int64_t sb = tr.seg_offsets[m];
+        const int64_t po = tr.offsets[m];
+        const int npm = (int)(tr.offsets[m + 1] - po);
+        const int lg0 = (int)((g0 > sb ? g0 : sb) - sb);
+        const int64_t se = tr.seg_offsets[m + 1];
+        const int lg1 = (int)((g1 < se ? g1 : se) - sb);
+        const int st_lo = lg0 << kSegShift;
+        int st_hi = lg1 << kSegShift;
+        if (st_hi > npm - 1) st_hi = npm - 1;
+        if (st_lo >= st_hi) continue;  // uniform over the block
+        int first = st_lo, last = st_hi - 1;
+        if (tr.vhat[m].w != 0.0) inwindow_steps(tr.tx + po, st_lo, st_hi, P, px.w, &first, &last);
+        if (!active || last < first) {
+            first = 0x7fffffff;
+            last = -1;
+        }
+        const int lo = warp_min(first), hi = warp_max(last);
+        if (lo > hi) continue;  // uniform over the warp
+        const int start = lo & ~(kSegLen - 1);  // >= st_lo
+        const int n_pts = hi + 2 - start;       // points start .. hi+1
+        const int n_chunks = (n_pts + kSegLen - 1) >> kSegShift;
+        const double4_32a* txp = tr.tx + po;
+        warp_stage(&wb[0], tr, po + start, min(kSegLen, npm - start), lane);
+        Anchor A;
+        PointState p1, p2;
+        float comp = 0.0f, chain_err = 0.0f;
+        for (int c = 0; c < n_chunks; c++) {
+            const int p0 = start + (c << kSegShift);
+            if (c + 1 < n_chunks) {
+                warp_stage(&wb[(c + 1) & 1], tr, po + p0 + kSegLen,
+                           min(kSegLen, npm - (p0 + kSegLen)), lane);
+                asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            } else {
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            }
+            __syncwarp();
+            const WarpChunk& B = wb[c & 1];
+            {
+                Anchor An;
+                make_anchor(An, txp[p0], px);
+                if (c > 0) rebase(p1, A, An);
+                A = An;
+            }
+            const int n_here = min(kSegLen, n_pts - (c << kSegShift));
+            for (int l = 0; l < n_here; l++) {
+                const int i = p0 + l;
+                point_field(p2, B.q0[l], B.q1[l], B.q2[l], A);
+                if (l == 0) {
+                    start_chain(p2, A);
+                    comp = 0.0f;
+                    chain_err = 0.0f;
+                } else {
+                    const float du = step_increment(p1, p2, B.q3[l - 1], px.kdt);
+                    chain_step(p1, p2, du, comp);
+                    chain_err += fabsf(du) * kChainRel + 1.0e-7f;
+                }
+                if (decide(p2, A.err + chain_err, txp, i, px, A)) nfb++;
+                if (i > start && active) {
+                    if (deposit_step32(p1, p2, A.Bi, sc.nt, sink)) inwin++;
+                }
+                p1 = p2;
+            }
+            __syncwarp();  // the buffer is restaged two chunks later
+        }
+    }
+    sink.flush();
+    if (sink.err) atomicOr(wk.status, sink.err);
+    inwin = warp_sum_u64(active ? inwin : 0);
+    nfb = warp_sum_u64(active ? nfb : 0);
+    unsigned long long nadd = warp_sum_u64(sink.n_add);
+    if (lane == 0 && wk.counters) {
+        if (inwin) atomicAdd(wk.counters, inwin);
+        if (nfb) atomicAdd(wk.counters + 1, nfb);
+        if (nadd) atomicAdd(wk.counters + 2, nadd);
+    }
+}
+
+cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
+                             cudaStream_t s) {
+    dim3 grid((sc.np + kWThreads - 1) / kWThreads, w.n_slots);
+    lw_fp32_warp_kernel<<<grid, kWThreads, 0, s>>>(tr, sc, w);
+    return cudaGetLastError();
+}
+
+}  // namespace teufel

@@ -68,6 +68,8 @@ constexpr int kVariantUniform = 0;
 constexpr int kVariantLanes = 1;
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
+cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
+                             cudaStream_t s);
 cudaError_t launch_fp64(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
                         cudaStream_t s);
 cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* out,
