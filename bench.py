@@ -55,6 +55,8 @@ def parse():
                     help="particle-range slots per launch (0 = library default)")
     ap.add_argument("--nots", type=int, default=0,
                     help="trace samples (0 = the workload's 4096); only for small profiling runs")
+    ap.add_argument("--variant", type=int, default=0,
+                    help="FP32 kernel variant (teufel_options.kernel_variant; 0 = automatic)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -251,7 +253,8 @@ def run_gb300(args):
     def step(j, timing):
         sets[j % n_batches].integrate_screen_device(pos.data_ptr(), t0.data_ptr(), w0.dt, nots,
                                                     n_pix, out.data_ptr(), stream=sptr,
-                                                    timing=timing, n_slots=args.slots)
+                                                    timing=timing, n_slots=args.slots,
+                                                    variant=args.variant)
 
     peak32, peak32x2, peak64 = abi.probe_peaks()
     peak_fp32 = max(peak32, peak32x2)
@@ -263,18 +266,19 @@ def run_gb300(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     kernel_ms, reduce_ms, launches = 0.0, 0.0, 0
-    deposits, inwin, fallbacks = 0, 0, 0
+    deposits, inwin, fallbacks, evaluations = 0, 0, 0, 0
     barrier_sync()
     e0.record(stream)
     for j in range(W, W + K):
         step(j, True)
-        d, nl, km, rm = sets[j % n_batches].last_timing()
+        d, ne, nl, km, rm = sets[j % n_batches].last_timing()
         iw, fb, st = sets[j % n_batches].last_inwindow()
         abi.check(st, "integration")
         kernel_ms += km
         reduce_ms += rm
         launches += nl
         deposits += d
+        evaluations += ne
         inwin += iw
         fallbacks += fb
     e1.record(stream)
@@ -359,6 +363,8 @@ def run_gb300(args):
             "config": workload_config(args.batch, w0.n_pix, nots, npts,
                                       {"parallelism": f"pixel shards x{world}",
                                        "in_window_fraction": frac_in,
+                                       "point_evaluations_per_in_window_step":
+                                           evaluations / inwin if inwin else None,
                                        "exact_fallback_points": fallbacks}),
             "fp64_gpu": {"value": fp64_rate, "unit": UNIT,
                          "sample": f"{len(sub)} pixels (every 16th) x {args.batch} particles",

@@ -62,8 +62,9 @@ typedef struct teufel_options {
     int precision;        /* TEUFEL_PREC_*                                        */
     int device_pointers;  /* 1: pix_pos, pix_t0 and out are device pointers      */
     int n_slots;          /* particle-range slots reduced in FP64; 0 = automatic  */
-    int kernel_variant;   /* FP32 path: 0 = automatic, 1 = block-uniform steps,
-                             2 = per-pixel steps                                 */
+    int kernel_variant;   /* FP32 path: 0 = automatic, 1 = warp-uniform steps,
+                             2 = per-pixel steps, 3 = warp-uniform steps with
+                             registers sized for 3 resident blocks per SM      */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
 } teufel_options;
@@ -172,11 +173,14 @@ int teufel_cuda_last_inwindow(const teufel_traj_set *traj, int64_t *inwindow,
 
 /* Work and timing of the last integrate call on this handle: deposits =
  * bin contributions made (>= in-window steps; multi-bin steps add one per
- * extra bin), launches = kernels launched, and -- when it ran with
- * options.timing -- the summed CUDA-event durations of the integration
- * kernels and of the reduction kernels [ms].  Synchronizes the device. */
-int teufel_cuda_last_timing(const teufel_traj_set *traj, int64_t *deposits, int *launches,
-                            double *kernel_ms, double *reduce_ms);
+ * extra bin), evaluations = trajectory-point evaluations made (in-window
+ * points, plus the points a warp walks for its neighbouring pixels),
+ * launches = kernels launched, and -- when it ran with options.timing -- the
+ * summed CUDA-event durations of the integration kernels and of the
+ * reduction kernels [ms].  Synchronizes the device.  Any pointer may be NULL. */
+int teufel_cuda_last_timing(const teufel_traj_set *traj, int64_t *deposits,
+                            int64_t *evaluations, int *launches, double *kernel_ms,
+                            double *reduce_ms);
 
 /* Peak FMA throughput of the current device (TFLOP/s, FMA = 2 flops), each
  * measured with independent FMA chains: scalar FP32 (FFMA), packed two-wide

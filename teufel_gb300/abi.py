@@ -101,7 +101,7 @@ def lib():
         L.teufel_cuda_last_inwindow.restype = ctypes.c_int
         L.teufel_cuda_last_inwindow.argtypes = [_vp, _lp, _lp]
         L.teufel_cuda_last_timing.restype = ctypes.c_int
-        L.teufel_cuda_last_timing.argtypes = [_vp, _lp, _ip, _dp, _dp]
+        L.teufel_cuda_last_timing.argtypes = [_vp, _lp, _lp, _ip, _dp, _dp]
         L.teufel_cuda_integrate_screen_noalloc.restype = ctypes.c_int
         L.teufel_cuda_integrate_screen_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_double,
                                                            ctypes.c_int, ctypes.c_int, _vp, _vp]
@@ -235,16 +235,18 @@ class TrajSet:
         return int(iw.value), int(fb.value), st
 
     def last_timing(self):
-        """(deposits, kernel launches, integration-kernel ms, reduction ms)
-        of the last call; the times need timing=True on that call."""
+        """(deposits, point evaluations, kernel launches, integration-kernel
+        ms, reduction ms) of the last call; the times need timing=True on
+        that call."""
         dep = ctypes.c_int64(0)
+        nev = ctypes.c_int64(0)
         nl = ctypes.c_int(0)
         k = ctypes.c_double(0)
         r = ctypes.c_double(0)
-        check(lib().teufel_cuda_last_timing(self.handle, ctypes.byref(dep), ctypes.byref(nl),
-                                            ctypes.byref(k), ctypes.byref(r)),
+        check(lib().teufel_cuda_last_timing(self.handle, ctypes.byref(dep), ctypes.byref(nev),
+                                            ctypes.byref(nl), ctypes.byref(k), ctypes.byref(r)),
               "teufel_cuda_last_timing")
-        return int(dep.value), int(nl.value), float(k.value), float(r.value)
+        return int(dep.value), int(nev.value), int(nl.value), float(k.value), float(r.value)
 
     def point_decisions(self, m, pos, t0, dt, nots):
         n = int(self.n_points[m])

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(128, 4)
               sc.nt);
     const int64_t g0 = wk.slot_seg[slot], g1 = wk.slot_seg[slot + 1];
     int m = g0 < g1 ? particle_of_segment(tr.seg_offsets, tr.n_particles, g0) : tr.n_particles;
-    unsigned long long inwin = 0, nfb = 0;
+    unsigned long long inwin = 0, nfb = 0, nev = 0;
     for (; m < tr.n_particles && tr.seg_offsets[m] < g1; ++m) {
         const int64_t sb = tr.seg_offsets[m];
         const int64_t po = tr.offsets[m];
@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(128, 4)
         const int max_trips = warp_max(trips);
         if (max_trips == 0) continue;
         if (trips == 0) start = st_lo;
+        else nev += (unsigned long long)(trips + 1);
         const double4_32a* txp = tr.tx + po;
         const float4 *q0 = tr.q0 + po, *q1 = tr.q1 + po, *q2 = tr.q2 + po, *q3 = tr.q3 + po;
         Anchor A;
@@ -187,11 +188,15 @@ __global__ void __launch_bounds__(128, 4)
         for (int j = 0; j < max_trips; ++j) {
             const int i2 = start + j + 1;
             const bool live = j < trips;
-            const bool boundary = (i2 & (kSegLen - 1)) == 0;
-            if (boundary) {  // uniform: every lane's start is a segment boundary
-                const int i2c = i2 < npm ? i2 : ((npm - 1) & ~(kSegLen - 1));
+            // uniform: every lane's start is a segment boundary, so the lanes
+            // reach segment and chunk boundaries together
+            const bool boundary = (i2 & (kSegLen - 1)) == 0 ||
+                                  ((i2 & (kChunkLen - 1)) == 0 &&
+                                   warp_any_above(chain_err, kReanchorBound));
+            if (boundary) {
+                const int i2c = i2 < npm ? i2 : ((npm - 1) & ~(kChunkLen - 1));
                 Anchor An;
-                make_anchor(An, txp[i2c], px);
+                make_anchor(An, txp[i2c], txp[i2c & ~(kSegLen - 1)], px);
                 rebase(p1, A, An);
                 A = An;
             }
@@ -217,10 +222,12 @@ __global__ void __launch_bounds__(128, 4)
     inwin = warp_sum_u64(inwin);
     nfb = warp_sum_u64(nfb);
     unsigned long long nadd = warp_sum_u64(sink.n_add);
+    nev = warp_sum_u64(nev);
     if ((threadIdx.x & 31) == 0 && wk.counters) {
         if (inwin) atomicAdd(wk.counters, inwin);
         if (nfb) atomicAdd(wk.counters + 1, nfb);
         if (nadd) atomicAdd(wk.counters + 2, nadd);
+        if (nev) atomicAdd(wk.counters + 3, nev);
     }
 }
 
@@ -231,7 +238,7 @@ cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w
         lw_fp32_lanes_kernel<<<grid, 128, 0, s>>>(tr, sc, w);
         return cudaGetLastError();
     }
-    return launch_fp32_warp(tr, sc, w, s);
+    return launch_fp32_warp(tr, sc, w, variant, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,8 +288,10 @@ cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const dou
 
 // ---------------------------------------------------------------------------
 // Decision record for the parity tests: one thread per segment of particle
-// m walks its points as both kernels do (anchor, FP32 chain, decision).
-// u_est is the estimate before any exact fallback, band the bound used.
+// m walks its points as both kernels do (anchor, FP32 chain, decision), with
+// the longest chain they can run (a whole segment, no intermediate anchor),
+// so that the error bound is checked where it is widest.  u_est is the
+// estimate before any exact fallback, band the bound used.
 // ---------------------------------------------------------------------------
 __global__ void point_decisions_kernel(DevTraj tr, int m, double3 P, double t0, double dt,
                                        int nt, int64_t* idx, int* flags, double* u_est,

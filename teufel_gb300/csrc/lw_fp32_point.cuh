@@ -123,8 +123,14 @@ struct Anchor {
     float err;     // bound on the anchor's error plus the reference's rounding [bins]
 };
 
-__device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const PixelCtx& px) {
-    const double Dx = px.P.x - a.y, Dy = px.P.y - a.z, Dz = px.P.z - a.w;
+// Anchor of a chain that starts at trajectory point a, with positions measured
+// from point b (the first point of a's segment, to which the per-point
+// offsets e are relative).
+__device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const double4_32a b,
+                                            const PixelCtx& px) {
+    A.Dx = (float)(px.P.x - b.y);
+    A.Dy = (float)(px.P.y - b.z);
+    A.Dz = (float)(px.P.z - b.w);
     const double pa = fma(px.Ph.x, a.y, fma(px.Ph.y, a.z, px.Ph.z * a.w));  // P^.x
     const double L = px.Pn - pa;
     const double cx = a.z * px.Ph.z - a.w * px.Ph.y;
@@ -150,15 +156,15 @@ __device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, cons
     A.B = (long long)fl;
     A.Bi = (int)fl;
     A.frac = (float)(u - fl);
-    A.Dx = (float)Dx;
-    A.Dy = (float)Dy;
-    A.Dz = (float)Dz;
     // our rounding: t, P^.x/c and their sum, G/c, the sum with Tp, the scaling
     const float own = (float)((fabs(a.x) + fabs(pa) * ic + fabs(px.Tp) + G * ic) * px.inv_dt *
                               4.5e-16) +
                       (float)(fabs(u) * 4.5e-16) + 1.0e-7f;
     A.err = own + px.refb0 + (float)(fabs(a.x) * px.inv_dt * 4.5e-16);
     if (u != u0) A.err = 1.0f;  // clamped: resolve the segment exactly
+}
+__device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const PixelCtx& px) {
+    make_anchor(A, a, a, px);
 }
 
 struct PointState {
@@ -329,6 +335,50 @@ struct PrefetchSink {
     }
 };
 
+// The same contract without the prefetch: a closed bin is added to the
+// partial trace with fire-and-forget vector reductions (red.global.add on
+// float2), which the L2 performs, so the thread neither holds the bin's old
+// content in registers nor waits for it.  Each pixel row is written by one
+// thread only; the reductions are used for their latency, not for atomicity.
+struct RedSink {
+    float2 a[3];
+    int open;
+    int nt;
+    float* row;  // this pixel's partial trace, [nt][6]
+    unsigned int err;
+    unsigned int n_add;
+    __device__ void init(float* r, int n) {
+        row = r;
+        nt = n;
+        open = -1;
+        err = 0;
+        n_add = 0;
+    }
+    __device__ __forceinline__ void add(int k, const float2* f) {
+        if (k < 0 || k >= nt) {
+            err |= 1u << TEUFEL_ERR_RANGE;
+            return;
+        }
+        n_add++;
+        if (k == open) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) a[c] = add2(a[c], f[c]);
+        } else {
+            flush();
+            open = k;
+#pragma unroll
+            for (int c = 0; c < 3; c++) a[c] = f[c];
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        if (open < 0) return;
+        float2* p = reinterpret_cast<float2*>(row + (int64_t)open * 6);
+#pragma unroll
+        for (int c = 0; c < 3; c++) atomicAdd(p + c, a[c]);
+        open = -1;
+    }
+};
+
 // ---------------------------------------------------------------------------
 // The deposit of one step in bin units from (ki, r) coordinates on base Bi;
 // the same branch structure and weights as deposit_step (lw_common.cuh),
@@ -401,5 +451,17 @@ __device__ __forceinline__ bool deposit_step32(const PointState& p1, const Point
 }
 
 constexpr float kChainRel = 1.0e-6f;  // bound on the relative error of one FP32 increment
+
+// A chain is re-anchored in FP64 at the next chunk boundary once the error
+// bound of any lane of the warp exceeds kReanchorBound [bins]: the rounding
+// of the increments accumulates as a random walk (about 3e-7 |du| per step
+// when the transverse direction components are ~1e-2 and the angles ~1e-3),
+// so chains that advance by many bins per step are kept short, while chains
+// that advance slowly run to the end of their segment.
+constexpr float kReanchorBound = 2.7e-5f;
+__device__ __forceinline__ bool warp_any_above(float v, float limit) {
+    // non-negative floats order like their bit patterns
+    return __reduce_max_sync(0xffffffffu, __float_as_uint(v)) > __float_as_uint(limit);
+}
 
 }  // namespace teufel

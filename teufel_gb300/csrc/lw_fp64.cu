@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(128)
               sc.nt);
     const int64_t g0 = wk.slot_seg[slot], g1 = wk.slot_seg[slot + 1];
     int m = g0 < g1 ? particle_of_segment(tr.seg_offsets, tr.n_particles, g0) : tr.n_particles;
-    unsigned long long inwin = 0;
+    unsigned long long inwin = 0, nev = 0;
     for (; m < tr.n_particles && tr.seg_offsets[m] < g1; ++m) {
         const int64_t sb = tr.seg_offsets[m];
         const int64_t po = tr.offsets[m];
@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(128)
         if (last < first) continue;
         const double scale = field_scale(tr.charge[m]);
         Point64 p1, p2;
+        nev += (unsigned long long)(last - first + 2);
         eval_point64(p1, tr, po + first, scale, P, w);
         for (int s = first; s <= last; ++s) {
             eval_point64(p2, tr, po + s + 1, scale, P, w);
@@ -124,9 +125,11 @@ __global__ void __launch_bounds__(128)
     if (sink.err) atomicOr(wk.status, sink.err);
     inwin = warp_sum_u64(inwin);
     unsigned long long nadd = warp_sum_u64(sink.n_add);
+    nev = warp_sum_u64(nev);
     if ((threadIdx.x & 31) == 0 && wk.counters) {
         if (inwin) atomicAdd(wk.counters, inwin);
         if (nadd) atomicAdd(wk.counters + 2, nadd);
+        if (nev) atomicAdd(wk.counters + 3, nev);
     }
 }
 

@@ -16,8 +16,13 @@ constexpr double kEps0 = 8.854187817e-12;
 // Trajectory points are grouped into segments of kSegLen steps.  Segment k of
 // a particle owns steps [k*kSegLen, (k+1)*kSegLen) and its first point is the
 // FP64 anchor from which the FP32 path measures positions and arrival times.
-constexpr int kSegShift = 5;
+// Segments are also the unit in which particle ranges are split over slots.
+constexpr int kSegShift = 7;
 constexpr int kSegLen = 1 << kSegShift;
+// The warp kernel stages trajectory data into shared memory in chunks of
+// kChunkLen points; a chain may start at any chunk boundary.
+constexpr int kChunkShift = 5;
+constexpr int kChunkLen = 1 << kChunkShift;
 
 // Device view of a resident trajectory set.
 struct DevTraj {
@@ -55,21 +60,24 @@ struct DevWork {
     int64_t slot_stride;      // elements between slots
     unsigned int* status;     // bit mask of TEUFEL_ERR_* seen on the device
     unsigned long long* counters;  // [0] in-window triples, [1] exact-fallback points,
-                                   // [2] bin contributions (deposits)
+                                   // [2] bin contributions (deposits), [3] point
+                                   // evaluations (in window or walked for a neighbour)
 };
 
 }  // namespace teufel
 
 // Kernel launchers (defined in the .cu files)
 namespace teufel {
-// FP32 kernel variants: all pixels of a block walk the same steps (uniform),
-// or every pixel walks its own in-window steps (lanes).
+// FP32 kernel variants: the 32 pixels of a warp walk the same steps (warp,
+// registers sized for 2 or 3 resident blocks per SM), or every pixel walks
+// its own in-window steps (lanes).
 constexpr int kVariantUniform = 0;
 constexpr int kVariantLanes = 1;
+constexpr int kVariantWarp3 = 2;
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
-                             cudaStream_t s);
+                             int variant, cudaStream_t s);
 cudaError_t launch_fp64(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
                         cudaStream_t s);
 cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* out,

@@ -33,7 +33,7 @@ struct teufel_traj_set {
     size_t out_cap = 0;  // doubles
     unsigned int* d_status = nullptr;
     unsigned long long* d_counters = nullptr;
-    unsigned long long last_counters[3] = {0, 0, 0};
+    unsigned long long last_counters[4] = {0, 0, 0, 0};
     // kernel timing of the last call (options.timing)
     std::vector<cudaEvent_t> ev;
     int n_ev_used = 0;
@@ -166,7 +166,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     TRY_CUDA(cudaMemcpyAsync(h->slot_seg, bounds.data(), sizeof(int64_t) * (slots_total + 1),
                              cudaMemcpyHostToDevice, s));
     TRY_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), s));
-    TRY_CUDA(cudaMemsetAsync(h->d_counters, 0, 3 * sizeof(unsigned long long), s));
+    TRY_CUDA(cudaMemsetAsync(h->d_counters, 0, sizeof(h->last_counters), s));
     h->n_ev_used = 0;
     h->last_launches = 0;
     h->last_timed = opt.timing != 0;
@@ -190,8 +190,9 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used], s));
         cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
                              : launch_fp32(h->dev, sc, w,
-                                           opt.kernel_variant == 2 ? kVariantLanes
-                                                                   : kVariantUniform,
+                                           opt.kernel_variant == 2   ? kVariantLanes
+                                           : opt.kernel_variant == 3 ? kVariantWarp3
+                                                                     : kVariantUniform,
                                            s);
         if (e != cudaSuccess) return cuda_fail(e);
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 1], s));
@@ -298,7 +299,7 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
         (rc = dev_alloc(h, &p_q3, N)))
         return fail(rc);
     if (cudaMalloc(&h->d_status, sizeof(unsigned int)) != cudaSuccess ||
-        cudaMalloc(&h->d_counters, 3 * sizeof(unsigned long long)) != cudaSuccess)
+        cudaMalloc(&h->d_counters, sizeof(h->last_counters)) != cudaSuccess)
         return fail(cuda_fail(cudaErrorMemoryAllocation));
     d.offsets = p_off;
     d.seg_offsets = p_seg;
@@ -377,7 +378,7 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     if (opt_in) opt = *opt_in;
     if (opt.precision != TEUFEL_PREC_FP32_SPLIT && opt.precision != TEUFEL_PREC_FP64)
         return TEUFEL_ERR_ARG;
-    h->last_counters[0] = h->last_counters[1] = h->last_counters[2] = 0;
+    for (auto& c : h->last_counters) c = 0;
     h->last_launches = 0;
     h->n_ev_used = 0;
     // the reference returns early for traces shorter than 2 samples and for
@@ -436,8 +437,9 @@ int teufel_cuda_last_inwindow(const teufel_traj_set* traj, int64_t* inwindow,
     return status_from_mask(mask);
 }
 
-int teufel_cuda_last_timing(const teufel_traj_set* traj, int64_t* deposits, int* launches,
-                            double* kernel_ms, double* reduce_ms) {
+int teufel_cuda_last_timing(const teufel_traj_set* traj, int64_t* deposits,
+                            int64_t* evaluations, int* launches, double* kernel_ms,
+                            double* reduce_ms) {
     if (!traj) return TEUFEL_ERR_ARG;
     teufel_traj_set* h = const_cast<teufel_traj_set*>(traj);
     if (cudaDeviceSynchronize() != cudaSuccess) return cuda_fail(cudaGetLastError());
@@ -456,6 +458,7 @@ int teufel_cuda_last_timing(const teufel_traj_set* traj, int64_t* deposits, int*
         }
     }
     if (deposits) *deposits = (int64_t)h->last_counters[2];
+    if (evaluations) *evaluations = (int64_t)h->last_counters[3];
     if (launches) *launches = h->last_launches;
     if (kernel_ms) *kernel_ms = k;
     if (reduce_ms) *reduce_ms = r;
