@@ -247,31 +247,6 @@ __device__ __forceinline__ void chain_step(const PointState& p1, PointState& p2,
     p2.ki = p1.ki + (int)k;
 }
 
-// Bin decision from (ki, r); falls back to the reference's exact FP64
-// evaluation when r is within `band` of +-1/2.
-__device__ __forceinline__ bool decide(PointState& S, float band, const double4_32a* tx,
-                                       int64_t i, const PixelCtx& px, const Anchor& A) {
-    const float d = 0.5f - fabsf(S.r);  // distance to the nearest half-integer
-    if (d <= band) {
-        const double ts = exact_retarded_time(tx[i], px.P);
-        S.idx = exact_bin(ts, px.w);
-        S.flags = exact_flags(ts, px.w);
-        // continue from the exact value
-        double v = (ts - px.w.t0) * px.inv_dt - (double)A.B;
-        v = fmax(-kBinLimit, fmin(v, kBinLimit));
-        const double k = floor(v + 0.5);
-        S.ki = (int)k;
-        S.r = (float)(v - k);
-        return true;
-    }
-    int k = A.Bi + S.ki;
-    const int nt = px.w.nt;
-    k = k < -2 ? -2 : (k > nt + 1 ? nt + 1 : k);
-    S.idx = k;
-    S.flags = (k < 0 ? kLeTmin : 0) | (k < nt ? kLtTmax : 0);
-    return false;
-}
-
 // Start a compensated arrival chain at an anchor point.
 __device__ __forceinline__ void start_chain(PointState& S, const Anchor& A) {
     const float k = rintf(A.frac);  // 0 or 1
@@ -377,6 +352,29 @@ struct RedSink {
         for (int c = 0; c < 3; c++) atomicAdd(p + c, a[c]);
         open = -1;
     }
+    // A regular step: f1 goes to bin k, in [0, nt); when `split`, f2 goes to
+    // bin k+1, also in [0, nt).  In a chain of regular steps bin k is
+    // already open, so the common work is the register accumulation.
+    __device__ __forceinline__ void add_fast(int k, bool split, const float2* f1,
+                                             const float2* f2) {
+        if (k != open) {
+            flush();
+            open = k;
+#pragma unroll
+            for (int c = 0; c < 3; c++) a[c] = make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) a[c] = add2(a[c], f1[c]);
+        if (split) {
+            float2* p = reinterpret_cast<float2*>(row + (int64_t)k * 6);
+#pragma unroll
+            for (int c = 0; c < 3; c++) atomicAdd(p + c, a[c]);
+            open = k + 1;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) a[c] = split ? f2[c] : a[c];
+        n_add += split ? 2u : 1u;
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -402,7 +400,7 @@ __device__ __forceinline__ bool deposit_step32(const PointState& p1, const Point
         // bins of the reference (src/particle.cpp:835-862), in one form.
         const bool split = idx2 > p1.idx;
         const float a = split ? (float)(p1.idx - u1i) + 0.5f - p1.r : dts;  // e' - u1
-        const float2 lam = splat2(a * rd);
+        const float2 lam = splat2(split ? a * rd : 1.0f);  // no 0/0 for a zero-length step
         float2 fe[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) fe[c] = fma2(sub2(p2.f[c], p1.f[c]), lam, p1.f[c]);
@@ -448,6 +446,84 @@ __device__ __forceinline__ bool deposit_step32(const PointState& p1, const Point
         sink.add(idx2, field);
     }
     return true;
+}
+
+// A regular step: both points resolved without the exact fallback, both bins
+// inside the trace (0 <= B + ki < nt, which implies ts > tmin and ts < tmax
+// since |r| stays below 1/2 by more than the error bound), and ki2 - ki1 in
+// {0, 1}.  deposit_step32 then takes its common branch with idx1 = B + ki1 and
+// a = 1/2 - r1; this is that branch without the flag and range logic.
+template <class Sink>
+__device__ __forceinline__ void deposit_fast(const PointState& p1, const PointState& p2, int Bi,
+                                             Sink& sink) {
+    const bool split = p2.ki != p1.ki;
+    const float dts = (split ? 1.0f : 0.0f) + (p2.r - p1.r);
+    const float a = split ? 0.5f - p1.r : dts;
+    const float2 lam = splat2(split ? a * __fdividef(1.0f, dts) : 1.0f);
+    float2 fe[3], field1[3], field2[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) fe[c] = fma2(sub2(p2.f[c], p1.f[c]), lam, p1.f[c]);
+    const float2 w1 = splat2(0.5f * a), w2 = splat2(0.5f * (dts - a));
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        field1[c] = mul2(add2(p1.f[c], fe[c]), w1);
+        field2[c] = mul2(add2(fe[c], p2.f[c]), w2);
+    }
+    sink.add_fast(Bi + p1.ki, split, field1, field2);
+}
+
+// Bin index and window flags of a point that was not resolved exactly, from
+// its chain coordinates (an exactly resolved point keeps its own).
+__device__ __forceinline__ void materialize(PointState& S, int Bi, int nt) {
+    if (S.flags & kExact) return;
+    int k = Bi + S.ki;
+    k = k < -2 ? -2 : (k > nt + 1 ? nt + 1 : k);
+    S.idx = k;
+    S.flags = (k < 0 ? kLeTmin : 0) | (k < nt ? kLtTmax : 0);
+}
+
+// The exact FP64 evaluation of a point whose estimate lies within its error
+// bound of a half-integer: the reference's bin index and window flags, and
+// the chain continued from the exact value (relative to anchor base B).
+// Kept out of line: it is rare, and its FP64 temporaries would otherwise
+// crowd the registers of the loop around it.
+struct ExactPoint {
+    int ki;
+    float r;
+    int idx;
+    int flags;
+};
+static __device__ __noinline__ ExactPoint exact_point(const double4_32a* tx, int64_t i,
+                                               const PixelCtx& px, int B) {
+    ExactPoint e;
+    const double ts = exact_retarded_time(tx[i], px.P);
+    e.idx = exact_bin(ts, px.w);
+    e.flags = exact_flags(ts, px.w);
+    double v = (ts - px.w.t0) * px.inv_dt - (double)B;
+    v = fmax(-kBinLimit, fmin(v, kBinLimit));
+    const double k = floor(v + 0.5);
+    e.ki = (int)k;
+    e.r = (float)(v - k);
+    return e;
+}
+__device__ __forceinline__ void apply_exact(PointState& S, const ExactPoint& e) {
+    S.ki = e.ki;
+    S.r = e.r;
+    S.idx = e.idx;
+    S.flags = e.flags;
+}
+
+// Bin decision from (ki, r); falls back to the reference's exact FP64
+// evaluation when r is within `band` of +-1/2.  Returns true on a fallback.
+__device__ __forceinline__ bool decide(PointState& S, float band, const double4_32a* tx,
+                                       int64_t i, const PixelCtx& px, const Anchor& A) {
+    if (0.5f - fabsf(S.r) <= band) {
+        apply_exact(S, exact_point(tx, i, px, A.Bi));
+        return true;
+    }
+    S.flags = 0;
+    materialize(S, A.Bi, px.w.nt);
+    return false;
 }
 
 constexpr float kChainRel = 1.0e-6f;  // bound on the relative error of one FP32 increment

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(kWThreads, MINB)
         Anchor A;
         PointState p1, p2;
         float comp = 0.0f, chain_err = 0.0f;
+        bool reg1 = false;
         for (int c = 0; c < n_chunks; c++) {
             const int p0 = start + (c << kChunkShift);
             if (c + 1 < n_chunks) {
@@ -130,10 +131,28 @@ __global__ void __launch_bounds__(kWThreads, MINB)
                     chain_step(p1, p2, du, comp);
                     chain_err += fabsf(du) * kChainRel + 1.0e-7f;
                 }
-                if (decide(p2, A.err + chain_err, txp, i, px, A)) nfb++;
-                if (i > start && active) {
+                bool reg2;
+                if (0.5f - fabsf(p2.r) <= A.err + chain_err) {
+                    apply_exact(p2, exact_point(txp, i, px, A.Bi));
+                    nfb++;
+                    reg2 = false;
+                } else {
+                    p2.flags = 0;
+                    reg2 = (unsigned)(A.Bi + p2.ki) < (unsigned)sc.nt;
+                }
+                const bool dep = i > start && active;
+                const bool fast = reg1 && reg2 && (unsigned)(p2.ki - p1.ki) <= 1u;
+                if (__all_sync(0xffffffffu, fast || !dep)) {
+                    if (dep) {
+                        deposit_fast(p1, p2, A.Bi, sink);
+                        inwin++;
+                    }
+                } else if (dep) {
+                    materialize(p1, A.Bi, sc.nt);
+                    materialize(p2, A.Bi, sc.nt);
                     if (deposit_step32(p1, p2, A.Bi, sc.nt, sink)) inwin++;
                 }
+                reg1 = reg2;
                 p1 = p2;
             }
             q3_last = B.q3[kChunkLen - 1];
