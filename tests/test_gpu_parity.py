@@ -72,7 +72,7 @@ def test_config1_fp64_matches_oracle(c1, c1_oracle):
     assert inwin > 0
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 4])
 def test_config1_fp32_matches_oracle(c1, c1_oracle, variant):
     with abi.TrajSet(c1.traj) as ts:
         g = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots, variant=variant)
@@ -173,7 +173,7 @@ def test_error_bound_holds(name, cfg, count, pix_step):
     print(f"{name}: largest |estimate - reference| / band = {worst:.3f} over {n_near} points")
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 4])
 @pytest.mark.parametrize("name,cfg,count,pix_step", [
     ("config2", H.config2, 48, 37),
     ("config4", H.config4, 6, 613),
@@ -215,6 +215,40 @@ def test_bunch_subset_parity(name, cfg, count, pix_step, variant):
         assert e < e_ref_ext + TOL_FP32, (name, e, e_ref_ext)
     else:
         assert e < TOL_FP32, (name, e)
+
+
+def _truncated(traj, lengths):
+    """The first lengths[m] points of each particle m of traj (cycling
+    through its particles)."""
+    o = traj.offsets
+    ts, xs, ps, as_, n, q, ms = [], [], [], [], [], [], []
+    for k, L in enumerate(lengths):
+        m = k % traj.n_particles
+        L = min(L, int(traj.n_points[m]))
+        sl = slice(o[m], o[m] + L)
+        ts.append(traj.t[sl]); xs.append(traj.x[sl]); ps.append(traj.p[sl]); as_.append(traj.a[sl])
+        n.append(L); q.append(traj.charge[m]); ms.append(traj.mass[m])
+    return H.Trajectories(np.concatenate(ts), np.concatenate(xs), np.concatenate(ps),
+                          np.concatenate(as_), np.array(n, np.int32), np.array(q),
+                          np.array(ms))
+
+
+@pytest.mark.parametrize("variant", [1, 2, 4])
+def test_uneven_particle_set(variant):
+    """An odd number of particles of unequal lengths, one with a single point
+    and one with none: the pair kernel pads the shorter particle of a pair
+    and leaves the last particle alone."""
+    w = _bunch_case(H.config2, 7, 41)
+    n = int(w.traj.n_points[0])
+    lengths = [n, int(0.6 * n), 1, n - 37, 0, int(0.3 * n), n - 129]
+    tr = _truncated(w.traj, lengths)
+    ref, rc = lw.integrate_screen(tr, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rc == 0 and np.abs(ref).max() > 0
+    with abi.TrajSet(tr) as ts:
+        g = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=variant)
+        _, _, st = ts.last_inwindow()
+    assert st == 0
+    assert rel_l2(g, ref) < TOL_FP32, rel_l2(g, ref)
 
 
 def test_charge_linearity(c1):

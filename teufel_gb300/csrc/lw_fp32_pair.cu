@@ -1,0 +1,591 @@
+// lw_fp32_pair.cu -- the split-precision kernel with two particles per
+// thread.
+//
+// As the warp-uniform kernel (lw_fp32_warp.cu), each warp owns 32 pixels and
+// walks trajectory points together, staged in shared memory.  Here every lane
+// carries two particles (a pair, 2j and 2j+1) for its pixel, and all the
+// per-point FP32 arithmetic -- the field, the arrival increment, the
+// compensated chain and the deposit weights -- is done on packed pairs
+// (add/sub/mul/fma.rn.f32x2), one instruction for both particles.  The
+// trajectory data of a pair is interleaved component by component when the
+// set is uploaded, so every operand pair comes straight out of shared memory.
+// Bin decisions, fallbacks and the sink stay per particle.
+//
+// Both particles deposit into the lane's one pixel row; each keeps its own
+// open bin.  A bin that both happen to hold open is added to twice by the
+// fire-and-forget reductions, which is the sum the trace needs.
+#include <cuda_runtime.h>
+
+#include "lw_fp32_point.cuh"
+
+namespace teufel {
+
+// ---------------------------------------------------------------------------
+// Preparation: the interleaved per-point data of every pair.
+// ---------------------------------------------------------------------------
+__global__ void prep_pairs_kernel(DevTraj tr, float4* pq) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = tr.pair_offsets[tr.n_pairs];
+    if (i >= total) return;
+    int lo = 0, hi = tr.n_pairs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tr.pair_offsets[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const int j = lo;
+    const int64_t l = i - tr.pair_offsets[j];
+    const int ma = 2 * j, mb = 2 * j + 1 < tr.n_particles ? 2 * j + 1 : 2 * j;
+    const int64_t oa = tr.offsets[ma], na = tr.offsets[ma + 1] - oa;
+    const int64_t ob = tr.offsets[mb], nb = tr.offsets[mb + 1] - ob;
+    float4 a0, a1, a2, a3, b0, b1, b2, b3;
+    if (na > 0) {
+        const int64_t k = oa + (l < na ? l : na - 1);
+        a0 = tr.q0[k]; a1 = tr.q1[k]; a2 = tr.q2[k]; a3 = tr.q3[k];
+    } else {
+        a0 = a1 = a2 = a3 = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
+    }
+    if (nb > 0) {
+        const int64_t k = ob + (l < nb ? l : nb - 1);
+        b0 = tr.q0[k]; b1 = tr.q1[k]; b2 = tr.q2[k]; b3 = tr.q3[k];
+    } else {
+        b0 = a0; b1 = a1; b2 = a2; b3 = a3;
+    }
+    float4* o = pq + 8 * i;
+    o[0] = make_float4(a0.x, b0.x, a0.y, b0.y);
+    o[1] = make_float4(a0.z, b0.z, a0.w, b0.w);
+    o[2] = make_float4(a1.x, b1.x, a1.y, b1.y);
+    o[3] = make_float4(a1.z, b1.z, a1.w, b1.w);
+    o[4] = make_float4(a2.x, b2.x, a2.y, b2.y);
+    o[5] = make_float4(a2.z, b2.z, a2.w, b2.w);
+    o[6] = make_float4(a3.x, b3.x, a3.y, b3.y);
+    o[7] = make_float4(a3.z, b3.z, a3.w, b3.w);
+}
+
+cudaError_t launch_prep_pairs(const DevTraj& tr, cudaStream_t s) {
+    if (tr.n_pairs <= 0) return cudaSuccess;
+    // the pair-point count is read on the device; launch for an upper bound
+    const int64_t bound = tr.n_points;  // >= sum over pairs of max(na, nb)
+    prep_pairs_kernel<<<(unsigned)((bound + 255) / 256), 256, 0, s>>>(tr,
+                                                                     const_cast<float4*>(tr.pq));
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Packed pairs: .x is particle a, .y particle b.
+// ---------------------------------------------------------------------------
+struct F2 {
+    float2 v;
+};
+__device__ __forceinline__ F2 f2(float a, float b) { return F2{make_float2(a, b)}; }
+__device__ __forceinline__ F2 f2(float2 a) { return F2{a}; }
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2{add2(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2{sub2(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2{mul2(a.v, b.v)}; }
+__device__ __forceinline__ F2 fma(F2 a, F2 b, F2 c) { return F2{fma2(a.v, b.v, c.v)}; }
+__device__ __forceinline__ F2 rsqrt2(F2 a) { return f2(rsqrtf(a.v.x), rsqrtf(a.v.y)); }
+__device__ __forceinline__ F2 rcp2(F2 a) {
+    return f2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y));
+}
+struct V2 {
+    F2 x, y, z;
+};
+__device__ __forceinline__ V2 cross(const V2& a, const V2& b) {
+    return V2{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ F2 dot(const V2& a, const V2& b) {
+    return fma(a.x, b.x, fma(a.y, b.y, a.z * b.z));
+}
+__device__ __forceinline__ V2 operator+(const V2& a, const V2& b) {
+    return V2{a.x + b.x, a.y + b.y, a.z + b.z};
+}
+__device__ __forceinline__ V2 operator-(const V2& a, const V2& b) {
+    return V2{a.x - b.x, a.y - b.y, a.z - b.z};
+}
+__device__ __forceinline__ V2 operator*(const V2& a, F2 s) { return V2{a.x * s, a.y * s, a.z * s}; }
+
+// The 8 float4 of one pair-point, as staged in shared memory.
+struct PairPoint {
+    float4 d[8];
+};
+__device__ __forceinline__ F2 lo2(float4 v) { return f2(v.x, v.y); }
+__device__ __forceinline__ F2 hi2(float4 v) { return f2(v.z, v.w); }
+
+struct PointState2 {
+    int ka, kb;     // ki of particles a, b
+    F2 r;
+    int idxa, idxb; // bin indices (general path only)
+    int fla, flb;   // window flags; kExact when resolved exactly, else 0 until materialized
+    V2 N;
+    F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
+};
+
+struct Anchor2 {
+    Anchor a, b;
+    V2 D;
+    F2 err;
+};
+__device__ __forceinline__ void pack_anchor(Anchor2& A) {
+    A.D = V2{f2(A.a.Dx, A.b.Dx), f2(A.a.Dy, A.b.Dy), f2(A.a.Dz, A.b.Dz)};
+    A.err = f2(A.a.err, A.b.err);
+}
+
+// point_field (lw_fp32_point.cuh) for both particles at once.
+__device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
+                                             const Anchor2& A) {
+    const V2 e{lo2(q.d[0]), hi2(q.d[0]), lo2(q.d[1])};
+    const V2 b{lo2(q.d[2]), hi2(q.d[2]), lo2(q.d[3])};
+    const F2 eps = hi2(q.d[3]);
+    const V2 c{lo2(q.d[4]), hi2(q.d[4]), lo2(q.d[5])};
+    const F2 cw = hi2(q.d[5]);
+    const F2 one = f2(1.0f, 1.0f);
+    const V2 D = A.D - e;
+    const F2 iR = rsqrt2(dot(D, D));
+    const V2 N = D * iR;
+    S.N = N;
+    const V2 W = cross(b, N);
+    const F2 rc1 = rcp2(one + dot(b, N));
+    const F2 kappa = fma((one - eps) * dot(W, W), rc1, eps);
+    const V2 Sv = N + b;
+    const V2 T = cross(W, Sv);
+    const V2 mb{fma(T.x, rc1, b.x * eps), fma(T.y, rc1, b.y * eps), fma(T.z, rc1, b.z * eps)};
+    const F2 rk = rcp2(kappa);
+    const F2 irk2 = iR * rk * rk;
+    const F2 cacc = irk2 * rk;
+    const F2 su = fma(cacc, dot(N, c), cw * iR * cacc);
+    const V2 E = mb * su - c * irk2;
+    const V2 Bv = cross(N, E);
+    S.f[0] = E.x;
+    S.f[1] = E.y;
+    S.f[2] = E.z;
+    S.f[3] = Bv.x;
+    S.f[4] = Bv.y;
+    S.f[5] = Bv.z;
+}
+
+// step_increment for both particles; q is the pair-point the step starts at.
+__device__ __forceinline__ F2 step_increment2(const PointState2& p1, const PointState2& p2,
+                                              const PairPoint& q, F2 kdt) {
+    const V2 ch{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])};
+    const F2 ceps = hi2(q.d[7]);
+    const F2 dt = hi2(q.d[1]);
+    const V2 s = p1.N + p2.N;
+    const V2 d = p1.N - p2.N;
+    const V2 w = cross(ch, s);
+    const F2 den = fma(f2(2.0f, 2.0f), dot(ch, s), f2(4.0f, 4.0f));
+    const F2 one_m_cos = dot(w, w) * rcp2(den);
+    const F2 one_m_n = f2(0.125f, 0.125f) * dot(d, d);
+    const F2 kap = fma(f2(1.0f, 1.0f) - ceps, one_m_n + one_m_cos, ceps);
+    return dt * kdt * kap;
+}
+
+__device__ __forceinline__ void chain_step2(const PointState2& p1, PointState2& p2, F2 du,
+                                            F2& comp) {
+    const F2 y = du - comp;
+    F2 t = p1.r + y;
+    comp = (t - p1.r) - y;
+    const float tx = fminf(fmaxf(t.v.x, -4.0e8f), 4.0e8f);
+    const float ty = fminf(fmaxf(t.v.y, -4.0e8f), 4.0e8f);
+    const float kx = rintf(tx), ky = rintf(ty);
+    p2.r = f2(tx, ty) - f2(kx, ky);
+    p2.ka = p1.ka + (int)kx;
+    p2.kb = p1.kb + (int)ky;
+}
+
+__device__ __forceinline__ void start_chain2(PointState2& S, const Anchor2& A) {
+    const float kx = rintf(A.a.frac), ky = rintf(A.b.frac);
+    S.ka = (int)kx;
+    S.kb = (int)ky;
+    S.r = f2(A.a.frac - kx, A.b.frac - ky);
+}
+
+// One particle of a pair as a PointState, for the general deposit.
+template <int W>
+__device__ __forceinline__ PointState unpack(const PointState2& S) {
+    PointState p;
+    p.ki = W ? S.kb : S.ka;
+    p.r = W ? S.r.v.y : S.r.v.x;
+    p.idx = W ? S.idxb : S.idxa;
+    p.flags = W ? S.flb : S.fla;
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        p.f[c] = W ? make_float2(S.f[2 * c].v.y, S.f[2 * c + 1].v.y)
+                   : make_float2(S.f[2 * c].v.x, S.f[2 * c + 1].v.x);
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// The sink of a lane: one pixel row, an open bin per particle, accumulators
+// in packed form (component c of particles a and b).  Closed bins are added
+// with fire-and-forget reductions, as RedSink (lw_fp32_point.cuh) does.
+// ---------------------------------------------------------------------------
+struct PairSink {
+    F2 acc[6];
+    int open_a, open_b;
+    int nt;
+    float* row;
+    unsigned int err;
+    unsigned int n_add;
+    __device__ void init(float* r, int n) {
+        row = r;
+        nt = n;
+        open_a = open_b = -1;
+        err = 0;
+        n_add = 0;
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[c] = f2(0.0f, 0.0f);
+    }
+    template <int W>
+    __device__ __forceinline__ float get(int c) const {
+        return W ? acc[c].v.y : acc[c].v.x;
+    }
+    template <int W>
+    __device__ __forceinline__ void set(int c, float v) {
+        if (W) acc[c].v.y = v; else acc[c].v.x = v;
+    }
+    template <int W>
+    __device__ __forceinline__ void reduce_to(int k) {
+        float2* p = reinterpret_cast<float2*>(row + (int64_t)k * 6);
+        atomicAdd(p, make_float2(get<W>(0), get<W>(1)));
+        atomicAdd(p + 1, make_float2(get<W>(2), get<W>(3)));
+        atomicAdd(p + 2, make_float2(get<W>(4), get<W>(5)));
+    }
+    template <int W>
+    __device__ __forceinline__ void flush() {
+        int& open = W ? open_b : open_a;
+        if (open < 0) return;
+        reduce_to<W>(open);
+        open = -1;
+    }
+    // The RedSink contract for particle W: f = component pairs (Ex,Ey),
+    // (Ez,cBx), (cBy,cBz).
+    template <int W>
+    __device__ __forceinline__ void add(int k, const float2* f) {
+        if (k < 0 || k >= nt) {
+            err |= 1u << TEUFEL_ERR_RANGE;
+            return;
+        }
+        n_add++;
+        int& open = W ? open_b : open_a;
+        if (k == open) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                set<W>(2 * c, get<W>(2 * c) + f[c].x);
+                set<W>(2 * c + 1, get<W>(2 * c + 1) + f[c].y);
+            }
+        } else {
+            flush<W>();
+            open = k;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                set<W>(2 * c, f[c].x);
+                set<W>(2 * c + 1, f[c].y);
+            }
+        }
+    }
+    // Regular steps of both particles: fa/fb say which particle deposits
+    // (its fields are zero otherwise), ka/kb its bin, sa/sb whether the step
+    // crosses into bin k+1.
+    __device__ __forceinline__ void add_fast(bool fa, bool fb, int ka, int kb, bool sa, bool sb,
+                                             const F2* f1, const F2* f2v) {
+        if (fa && ka != open_a) {
+            flush<0>();
+            open_a = ka;
+#pragma unroll
+            for (int c = 0; c < 6; c++) acc[c].v.x = 0.0f;
+        }
+        if (fb && kb != open_b) {
+            flush<1>();
+            open_b = kb;
+#pragma unroll
+            for (int c = 0; c < 6; c++) acc[c].v.y = 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[c] = acc[c] + f1[c];
+        if (sa) {
+            reduce_to<0>(ka);
+            open_a = ka + 1;
+        }
+        if (sb) {
+            reduce_to<1>(kb);
+            open_b = kb + 1;
+        }
+        const F2 keep = f2(sa ? 0.0f : 1.0f, sb ? 0.0f : 1.0f);
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, f2v[c]);
+        n_add += (unsigned)fa + (unsigned)fb + (unsigned)sa + (unsigned)sb;
+    }
+};
+
+template <int W>
+struct PairView {
+    PairSink* s;
+    __device__ __forceinline__ void add(int k, const float2* f) { s->add<W>(k, f); }
+};
+
+// Regular steps of both particles (deposit_fast, lw_fp32_point.cuh, in packed
+// form).  fa/fb: the particle deposits a regular step.
+__device__ __forceinline__ void deposit_fast2(const PointState2& p1, const PointState2& p2,
+                                              int Ba, int Bb, bool fa, bool fb, PairSink& sink) {
+    const bool sa = fa && p2.ka != p1.ka, sb = fb && p2.kb != p1.kb;
+    const F2 dts = f2(sa ? 1.0f : 0.0f, sb ? 1.0f : 0.0f) + (p2.r - p1.r);
+    const F2 h = f2(0.5f, 0.5f) - p1.r;
+    const F2 a = f2(sa ? h.v.x : dts.v.x, sb ? h.v.y : dts.v.y);
+    const F2 rd = rcp2(dts);
+    const F2 lam = f2(sa ? a.v.x * rd.v.x : 1.0f, sb ? a.v.y * rd.v.y : 1.0f);
+    const F2 w1 = f2(fa ? 0.5f * a.v.x : 0.0f, fb ? 0.5f * a.v.y : 0.0f);
+    const F2 w2 = f2(0.5f, 0.5f) * (dts - a) * f2(sa ? 1.0f : 0.0f, sb ? 1.0f : 0.0f);
+    F2 field1[6], field2[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        const F2 fe = fma(p2.f[c] - p1.f[c], lam, p1.f[c]);
+        field1[c] = (p1.f[c] + fe) * w1;
+        field2[c] = (fe + p2.f[c]) * w2;
+    }
+    sink.add_fast(fa, fb, Ba + p1.ka, Bb + p1.kb, sa, sb, field1, field2);
+}
+
+// ---------------------------------------------------------------------------
+// The kernel
+// ---------------------------------------------------------------------------
+constexpr int kPThreads = 128;
+constexpr int kPWarps = kPThreads / 32;
+
+// A staged chunk: p[0] is the pair-point before the chunk (the start of the
+// chunk's first step), p[1 + l] the chunk's point l.
+struct __align__(16) PairChunk {
+    PairPoint p[kChunkLen + 1];
+};
+
+// The 32 lanes copy pair-points p0-1 .. p0+avail-1 of the pair whose data
+// starts at pq (p[0] only when p0 > 0).
+__device__ __forceinline__ void pair_stage(PairChunk* b, const float4* pq, int p0, int avail,
+                                           int lane) {
+    const int skip = p0 > 0 ? 0 : 8;  // float4s of p[0] not copied
+    const int n = 8 * (avail + 1);
+    const float4* src = pq + 8 * ((int64_t)p0 - 1);
+    float4* dst = reinterpret_cast<float4*>(b->p);
+#pragma unroll
+    for (int k = 0; k < (8 * (kChunkLen + 1) + 31) / 32; k++) {
+        const int t = lane + 32 * k;
+        if (t >= skip && t < n) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + t);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + t)
+                         : "memory");
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ int pair_of_segment(const int64_t* seg_offsets, int n, int64_t g) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (seg_offsets[mid + 1] > g) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+// In-window step range of particle m within local steps [st_lo, st_hi), or
+// an empty range (first > last) when the lane has none.
+__device__ __forceinline__ void particle_range(const DevTraj& tr, int m, int st_lo, int st_hi,
+                                               bool active, const double3& P, const Window& w,
+                                               int& first, int& last) {
+    first = 0x7fffffff;
+    last = -1;
+    if (!active || st_lo >= st_hi) return;
+    first = st_lo;
+    last = st_hi - 1;
+    if (tr.vhat[m].w != 0.0) inwindow_steps(tr.tx + tr.offsets[m], st_lo, st_hi, P, w, &first, &last);
+    if (last < first) {
+        first = 0x7fffffff;
+        last = -1;
+    }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kPThreads, MINB)
+    lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
+    __shared__ PairChunk buf[kPWarps][2];
+    __shared__ PixelCtx pxs[kPThreads];
+    const int slot = blockIdx.y;
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool active = pix < sc.np;
+    const int pc = active ? pix : sc.np - 1;
+    const double3 P = make_double3(sc.pix_pos[3 * pc], sc.pix_pos[3 * pc + 1],
+                                   sc.pix_pos[3 * pc + 2]);
+    pxs[threadIdx.x] = make_pixel(P, sc.pix_t0[pc], sc.dt, sc.nt);
+    const PixelCtx& px = pxs[threadIdx.x];
+    const F2 kdt = f2(px.kdt, px.kdt);
+    PairChunk* wb = buf[warp];
+    PairSink sink;
+    sink.init(static_cast<float*>(wk.scratch) + (int64_t)slot * wk.slot_stride +
+                  (int64_t)pc * sc.nt * 6,
+              sc.nt);
+    const int nt = sc.nt;
+    const int64_t g0 = wk.slot_seg[slot], g1 = wk.slot_seg[slot + 1];
+    int j = g0 < g1 ? pair_of_segment(tr.pair_seg_offsets, tr.n_pairs, g0) : tr.n_pairs;
+    unsigned long long inwin = 0, nfb = 0, nev = 0;
+    for (; j < tr.n_pairs && tr.pair_seg_offsets[j] < g1; ++j) {
+        const int64_t sb = tr.pair_seg_offsets[j];
+        const int64_t se = tr.pair_seg_offsets[j + 1];
+        const int lg0 = (int)((g0 > sb ? g0 : sb) - sb);
+        const int lg1 = (int)((g1 < se ? g1 : se) - sb);
+        const int ma = 2 * j;
+        const bool hasb = 2 * j + 1 < tr.n_particles;
+        const int mb = hasb ? 2 * j + 1 : ma;
+        const int npa = (int)(tr.offsets[ma + 1] - tr.offsets[ma]);
+        const int npb = hasb ? (int)(tr.offsets[mb + 1] - tr.offsets[mb]) : 0;
+        const int st_lo = lg0 << kSegShift;
+        const int st_hi_a = min(lg1 << kSegShift, npa - 1);
+        const int st_hi_b = min(lg1 << kSegShift, npb - 1);
+        int fa, la, fb, lb;
+        particle_range(tr, ma, st_lo, st_hi_a, active, P, px.w, fa, la);
+        particle_range(tr, mb, st_lo, hasb ? st_hi_b : st_lo, active, P, px.w, fb, lb);
+        const int lo = warp_min(min(fa, fb)), hi = warp_max(max(la, lb));
+        if (lo > hi) continue;  // uniform over the warp
+        const int start = lo & ~(kChunkLen - 1);  // >= st_lo, a segment boundary
+        const int n_pts = hi + 2 - start;           // points start .. hi+1
+        const int n_chunks = (n_pts + kChunkLen - 1) >> kChunkShift;
+        const int64_t po = tr.pair_offsets[j];
+        const int npp = (int)(tr.pair_offsets[j + 1] - po);
+        const double4_32a* txa = tr.tx + tr.offsets[ma];
+        const double4_32a* txb = tr.tx + tr.offsets[mb];
+        const float4* pqj = tr.pq + 8 * po;
+        pair_stage(&wb[0], pqj, start, min(kChunkLen, npp - start), lane);
+        Anchor2 A;
+        PointState2 p1, p2;
+        F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);
+        bool reg1a = false, reg1b = false;
+        for (int c = 0; c < n_chunks; c++) {
+            const int p0 = start + (c << kChunkShift);
+            if (c + 1 < n_chunks) {
+                pair_stage(&wb[(c + 1) & 1], pqj, p0 + kChunkLen,
+                           min(kChunkLen, npp - (p0 + kChunkLen)), lane);
+                asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            } else {
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            }
+            __syncwarp();
+            const PairChunk& B = wb[c & 1];
+            const bool anchor =
+                c == 0 || (p0 & (kSegLen - 1)) == 0 ||
+                warp_any_above(fmaxf(chain_err.v.x, chain_err.v.y), kReanchorBound);
+            if (anchor) {
+                Anchor2 An;
+                // past its last point a particle repeats it, with positions
+                // relative to that point's segment; a particle without points
+                // borrows its partner's anchor (it never deposits)
+                const int ia = min(p0, npa - 1), ib = min(p0, npb - 1);
+                if (npa > 0) make_anchor(An.a, txa[ia], txa[ia & ~(kSegLen - 1)], px);
+                if (hasb && npb > 0) make_anchor(An.b, txb[ib], txb[ib & ~(kSegLen - 1)], px);
+                else An.b = An.a;
+                if (npa <= 0) An.a = An.b;
+                pack_anchor(An);
+                if (c > 0) {
+                    p1.ka += A.a.Bi - An.a.Bi;  // rebase: B + ki is unchanged
+                    p1.kb += A.b.Bi - An.b.Bi;
+                }
+                A = An;
+            }
+            const int n_here = min(kChunkLen, n_pts - (c << kChunkShift));
+            for (int l = 0; l < n_here; l++) {
+                const int i = p0 + l;
+                point_field2(p2, B.p[l + 1], A);
+                if (l == 0 && anchor) {
+                    start_chain2(p2, A);
+                    comp = f2(0.0f, 0.0f);
+                    chain_err = f2(0.0f, 0.0f);
+                } else {
+                    const F2 du = step_increment2(p1, p2, B.p[l], kdt);
+                    chain_step2(p1, p2, du, comp);
+                    chain_err = fma(f2(fabsf(du.v.x), fabsf(du.v.y)),
+                                    f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));
+                }
+                const F2 band = A.err + chain_err;
+                const bool dep_a = active && i > start && i <= st_hi_a;
+                const bool dep_b = active && hasb && i > start && i <= st_hi_b;
+                bool reg2a, reg2b;
+                if (0.5f - fabsf(p2.r.v.x) <= band.v.x && i < npa) {
+                    const ExactPoint e = exact_point(txa, i, px, A.a.Bi);
+                    p2.ka = e.ki;
+                    p2.r.v.x = e.r;
+                    p2.idxa = e.idx;
+                    p2.fla = e.flags;
+                    nfb++;
+                    reg2a = false;
+                } else {
+                    p2.fla = 0;
+                    reg2a = (unsigned)(A.a.Bi + p2.ka) < (unsigned)nt;
+                }
+                if (0.5f - fabsf(p2.r.v.y) <= band.v.y && hasb && i < npb) {
+                    const ExactPoint e = exact_point(txb, i, px, A.b.Bi);
+                    p2.kb = e.ki;
+                    p2.r.v.y = e.r;
+                    p2.idxb = e.idx;
+                    p2.flb = e.flags;
+                    nfb++;
+                    reg2b = false;
+                } else {
+                    p2.flb = 0;
+                    reg2b = (unsigned)(A.b.Bi + p2.kb) < (unsigned)nt;
+                }
+                const bool fast_a = reg1a && reg2a && (unsigned)(p2.ka - p1.ka) <= 1u;
+                const bool fast_b = reg1b && reg2b && (unsigned)(p2.kb - p1.kb) <= 1u;
+                // steps that certainly lie outside the window: nothing to add
+                const bool out_a = (p2.fla == 0 && A.a.Bi + p2.ka < 0) ||
+                                   (!(p1.fla & kExact) && A.a.Bi + p1.ka >= nt);
+                const bool out_b = (p2.flb == 0 && A.b.Bi + p2.kb < 0) ||
+                                   (!(p1.flb & kExact) && A.b.Bi + p1.kb >= nt);
+                const bool ok = (!dep_a || fast_a || out_a) && (!dep_b || fast_b || out_b);
+                if (__all_sync(0xffffffffu, ok)) {
+                    const bool da = dep_a && fast_a, db = dep_b && fast_b;
+                    if (da || db) deposit_fast2(p1, p2, A.a.Bi, A.b.Bi, da, db, sink);
+                    inwin += (unsigned)da + (unsigned)db;
+                } else {
+                    if (dep_a) {
+                        PointState q1 = unpack<0>(p1), q2 = unpack<0>(p2);
+                        materialize(q1, A.a.Bi, nt);
+                        materialize(q2, A.a.Bi, nt);
+                        PairView<0> v{&sink};
+                        if (deposit_step32(q1, q2, A.a.Bi, nt, v)) inwin++;
+                    }
+                    if (dep_b) {
+                        PointState q1 = unpack<1>(p1), q2 = unpack<1>(p2);
+                        materialize(q1, A.b.Bi, nt);
+                        materialize(q2, A.b.Bi, nt);
+                        PairView<1> v{&sink};
+                        if (deposit_step32(q1, q2, A.b.Bi, nt, v)) inwin++;
+                    }
+                }
+                reg1a = reg2a;
+                reg1b = reg2b;
+                p1 = p2;
+            }
+            __syncwarp();  // the buffer is restaged two chunks later
+        }
+        if (active) nev += (unsigned long long)n_pts * (hasb ? 2u : 1u);
+    }
+    sink.flush<0>();
+    sink.flush<1>();
+    if (sink.err) atomicOr(wk.status, sink.err);
+    inwin = warp_sum_u64(active ? inwin : 0);
+    nfb = warp_sum_u64(active ? nfb : 0);
+    unsigned long long nadd = warp_sum_u64(sink.n_add);
+    nev = warp_sum_u64(nev);
+    if (lane == 0 && wk.counters) {
+        if (inwin) atomicAdd(wk.counters, inwin);
+        if (nfb) atomicAdd(wk.counters + 1, nfb);
+        if (nadd) atomicAdd(wk.counters + 2, nadd);
+        if (nev) atomicAdd(wk.counters + 3, nev);
+    }
+}
+
+cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
+                             cudaStream_t s) {
+    dim3 grid((sc.np + kPThreads - 1) / kPThreads, w.n_slots);
+    lw_fp32_pair_kernel<3><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+    return cudaGetLastError();
+}
+
+}  // namespace teufel

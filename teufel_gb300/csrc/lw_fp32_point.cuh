@@ -42,7 +42,11 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) {
     return r.f;
 }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    return add2(a, make_float2(-b.x, -b.y));
+    F2U x, y, r;
+    x.f = a;
+    y.f = b;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(x.u), "l"(y.u));
+    return r.f;
 }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
     F2U x, y, r;

@@ -41,6 +41,21 @@ struct DevTraj {
     const float4* q2;           // [Npts] A/gamma*scale/c (xyz), scale/gamma^2
     const float4* q3;           // [Npts] chord direction of the step from here (xyz),
                                 //        1 - |chord velocity|/c
+    // Particles 2j and 2j+1 form pair j (the last pair of an odd set has one
+    // particle).  A pair is as long as its longer particle; its per-point
+    // data interleaves the two particles' q0..q3 component by component,
+    // 8 float4 per pair-point:
+    //   (e.x a, e.x b, e.y a, e.y b) (e.z a, e.z b, dt a, dt b)
+    //   (bx a, bx b, by a, by b)     (bz a, bz b, eps a, eps b)
+    //   (cx a, cx b, cy a, cy b)     (cz a, cz b, cw a, cw b)
+    //   (chx a, chx b, chy a, chy b) (chz a, chz b, ceps a, ceps b)
+    // where b = beta-hat, c = q2, ch = chord direction; beyond the end of the
+    // shorter particle its last point is repeated.
+    int n_pairs;
+    int64_t n_pair_segments;
+    const int64_t* pair_offsets;      // [n_pairs+1] first pair-point of each pair
+    const int64_t* pair_seg_offsets;  // [n_pairs+1] first pair-segment of each pair
+    const float4* pq;                 // [pair-points][8]
 };
 
 // One observer handed to a kernel launch.
@@ -52,7 +67,8 @@ struct DevScreen {
     double dt;
 };
 
-// Work split: slot s integrates global segments [slot_seg[s], slot_seg[s+1]).
+// Work split: slot s integrates global segments [slot_seg[s], slot_seg[s+1])
+// (particle segments, or pair segments for the pair kernel).
 struct DevWork {
     int n_slots;
     const int64_t* slot_seg;  // [n_slots+1]
@@ -74,6 +90,7 @@ namespace teufel {
 constexpr int kVariantUniform = 0;
 constexpr int kVariantLanes = 1;
 constexpr int kVariantWarp3 = 2;
+constexpr int kVariantPair = 3;  // two particles per thread, packed FP32 pairs
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
@@ -91,6 +108,9 @@ cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const doubl
                                     const double* f, double t0, double dt, int nt, int precision,
                                     double* trace, unsigned int* status, cudaStream_t s);
 cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s);
+cudaError_t launch_prep_pairs(const DevTraj& tr, cudaStream_t s);
+cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
+                             cudaStream_t s);
 cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const double* ts,
                                       const double* f, double t0, double dt, int nt,
                                       double* trace, float* trace32, unsigned int* status,

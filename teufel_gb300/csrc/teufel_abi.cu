@@ -135,7 +135,16 @@ bool finite_array(const double* p, int64_t n) {
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
                int np, double* d_out, const teufel_options& opt, cudaStream_t s) {
     const bool fp64 = opt.precision == TEUFEL_PREC_FP64;
-    const int64_t G = h->dev.n_segments;
+    const int variant = opt.kernel_variant == 2   ? kVariantLanes
+                        : opt.kernel_variant == 3 ? kVariantWarp3
+                        : opt.kernel_variant == 4 ? kVariantPair
+                                                  : kVariantUniform;
+    const bool pairs = !fp64 && variant == kVariantPair;
+    // work units: particle segments, or pair segments for the pair kernel
+    const int64_t G = pairs ? h->dev.n_pair_segments : h->dev.n_segments;
+    const int64_t units = pairs ? h->dev.n_pairs : h->dev.n_particles;
+    const int64_t max_units_per_slot = pairs ? kMaxParticlesPerSlotFp32 / 2
+                                             : kMaxParticlesPerSlotFp32;
     const size_t elem = fp64 ? sizeof(double) : sizeof(float);
     const size_t slot_bytes = (size_t)np * (size_t)nt * 6 * elem;
     const int pix_blocks = (np + kThreads - 1) / kThreads;
@@ -144,8 +153,8 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                                            ((int64_t)pix_blocks * kThreads);
     int64_t slots_total = std::max<int64_t>(target, 1);
     if (!fp64 && opt.n_slots <= 0)
-        slots_total = std::max<int64_t>(
-            slots_total, (h->dev.n_particles + kMaxParticlesPerSlotFp32 - 1) / kMaxParticlesPerSlotFp32);
+        slots_total = std::max<int64_t>(slots_total,
+                                        (units + max_units_per_slot - 1) / max_units_per_slot);
     slots_total = std::min<int64_t>(slots_total, std::max<int64_t>(G, 1));
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -189,11 +198,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         w.counters = h->d_counters;
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used], s));
         cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
-                             : launch_fp32(h->dev, sc, w,
-                                           opt.kernel_variant == 2   ? kVariantLanes
-                                           : opt.kernel_variant == 3 ? kVariantWarp3
-                                                                     : kVariantUniform,
-                                           s);
+                             : launch_fp32(h->dev, sc, w, variant, s);
         if (e != cudaSuccess) return cuda_fail(e);
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 1], s));
         e = fp64 ? launch_reduce_fp64(w, sc, d_out, s) : launch_reduce_fp32(w, sc, d_out, s);
@@ -274,6 +279,16 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     }
     const int64_t N = offs[n_particles];
     if (N > 0 && (!t || !x || !bg || !a)) return TEUFEL_ERR_ARG;
+    // pairs (2j, 2j+1): as long as the longer particle
+    const int n_pairs = (n_particles + 1) / 2;
+    std::vector<int64_t> poffs(n_pairs + 1, 0), psegs(n_pairs + 1, 0);
+    for (int j = 0; j < n_pairs; j++) {
+        int np = n_points[2 * j];
+        if (2 * j + 1 < n_particles) np = std::max(np, n_points[2 * j + 1]);
+        poffs[j + 1] = poffs[j] + np;
+        psegs[j + 1] = psegs[j] + (np >= 1 ? ((int64_t)(np - 1) >> kSegShift) + 1 : 0);
+    }
+    const int64_t NP = poffs[n_pairs];
     if (!finite_array(charge_C, n_particles)) return TEUFEL_ERR_ARG;
     teufel_traj_set* h = new (std::nothrow) teufel_traj_set();
     if (!h) return TEUFEL_ERR_NOMEM;
@@ -287,7 +302,10 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     d.n_particles = n_particles;
     d.n_points = N;
     d.n_segments = segs[n_particles];
-    int64_t *p_off, *p_seg;
+    d.n_pairs = n_pairs;
+    d.n_pair_segments = psegs[n_pairs];
+    int64_t *p_off, *p_seg, *p_poff, *p_pseg;
+    float4* p_pq;
     double* p_charge;
     double4_32a *p_vhat, *p_tx, *p_pp, *p_aa;
     float4 *p_q0, *p_q1, *p_q2, *p_q3;
@@ -296,7 +314,8 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
         (rc = dev_alloc(h, &p_tx, N)) || (rc = dev_alloc(h, &p_pp, N)) ||
         (rc = dev_alloc(h, &p_aa, N)) || (rc = dev_alloc(h, &p_q0, N)) ||
         (rc = dev_alloc(h, &p_q1, N)) || (rc = dev_alloc(h, &p_q2, N)) ||
-        (rc = dev_alloc(h, &p_q3, N)))
+        (rc = dev_alloc(h, &p_q3, N)) || (rc = dev_alloc(h, &p_poff, n_pairs + 1)) ||
+        (rc = dev_alloc(h, &p_pseg, n_pairs + 1)) || (rc = dev_alloc(h, &p_pq, 8 * NP)))
         return fail(rc);
     if (cudaMalloc(&h->d_status, sizeof(unsigned int)) != cudaSuccess ||
         cudaMalloc(&h->d_counters, sizeof(h->last_counters)) != cudaSuccess)
@@ -312,9 +331,14 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     d.q1 = p_q1;
     d.q2 = p_q2;
     d.q3 = p_q3;
+    d.pair_offsets = p_poff;
+    d.pair_seg_offsets = p_pseg;
+    d.pq = p_pq;
     cudaStream_t s = 0;
     if (cudaMemcpy(p_off, offs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
         cudaMemcpy(p_seg, segs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(p_poff, poffs.data(), sizeof(int64_t) * (n_pairs + 1), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(p_pseg, psegs.data(), sizeof(int64_t) * (n_pairs + 1), cudaMemcpyHostToDevice) ||
         (n_particles > 0 &&
          cudaMemcpy(p_charge, charge_C, sizeof(double) * n_particles, cudaMemcpyHostToDevice)) ||
         cudaMemset(h->d_status, 0, sizeof(unsigned int)))
@@ -335,6 +359,7 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
             e = cudaGetLastError();
         }
         if (!e) e = launch_prep_points(d, s);
+        if (!e) e = launch_prep_pairs(d, s);
         cudaError_t e2 = cudaStreamSynchronize(s);
         cudaFree(raw);
         if (e || e2) return fail(cuda_fail(e ? e : e2));
