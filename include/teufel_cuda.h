@@ -65,7 +65,8 @@ typedef struct teufel_options {
     int kernel_variant;   /* FP32 path: 0 = automatic, 1 = warp-uniform steps,
                              2 = per-pixel steps, 3 = warp-uniform steps with
                              registers sized for 3 resident blocks per SM,
-                             4 = warp-uniform steps, two particles per thread  */
+                             4 = warp-uniform steps, two particles per thread,
+                             5 = the same with registers for 12 warps per SM  */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
 } teufel_options;

@@ -19,6 +19,7 @@
 #pragma once
 
 #include <cstddef>
+#include <cstdio>
 #include <cstring>
 #include <exception>
 #include <string>
@@ -131,6 +132,7 @@ public:
     virtual std::size_t getBufferSize() = 0;
     virtual double* getBuffer() = 0;  // new[]-allocated, freed by the caller
     virtual void fromBuffer(double* buffer, std::size_t size) = 0;
+    virtual void generateOutput() = 0;
 };
 
 template <typename SourceT>
@@ -194,6 +196,11 @@ public:
             throw IOexception("ScreenObserver::fromBuffer() - buffer size mismatch.");
         std::memcpy(buf.data(), buffer, sizeof(double) * size);
     }
+    // The reference writes HDF5 here (ScreenObserver::WriteTimeDomainFieldHDF5 (src/screen.cpp:298-560)); this build
+    // has no HDF5 library, so the traces leave through getBuffer().
+    void generateOutput() override {
+        throw IOexception("ScreenObserver::generateOutput - HDF5 output is not available in this build");
+    }
     void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
 
 private:
@@ -239,6 +246,11 @@ public:
             throw IOexception("MeshedScreen::fromBuffer() - buffer size mismatch.");
         std::memcpy(buf.data(), buffer, sizeof(double) * size);
     }
+    // The reference writes HDF5 here (MeshedScreen::writeFile (src/mesh.cpp:428-736)); this build
+    // has no HDF5 library, so the traces leave through getBuffer().
+    void generateOutput() override {
+        throw IOexception("MeshedScreen::generateOutput - HDF5 output is not available in this build");
+    }
     void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
 
 private:
@@ -249,11 +261,56 @@ private:
     std::vector<double> buf;  // [Np][Nt][6]
 };
 
-// One observation point (src/point_observer.cpp:30-110).
+// The trace of one observation point as an SDDS (version 1) file in ASCII
+// mode, with the layout PointObserver::WriteTimeDomainFieldSDDS writes
+// (src/point_observer.cpp:120-181): parameters NumberTimeSteps (long), t0 and
+// dt (double); columns t [s], Ex, Ey, Ez [V/m] and Bx, By, Bz [T] (double);
+// one page of N rows.  Written from the SDDS format description; values carry
+// 17 significant digits, so they read back exactly.
+inline void write_trace_sdds(const std::string& filename, double t0, double dt, std::size_t N,
+                             const double* f) {
+    std::FILE* fp = std::fopen(filename.c_str(), "w");
+    if (!fp)
+        throw IOexception("PointObserver::WriteTimeDomainFieldSDDS - error in InitializeOutput()");
+    std::fprintf(fp, "SDDS1\n");
+    std::fprintf(fp, "&parameter name=NumberTimeSteps, type=long, &end\n");
+    std::fprintf(fp, "&parameter name=t0, type=double, &end\n");
+    std::fprintf(fp, "&parameter name=dt, type=double, &end\n");
+    const char* cols[7][3] = {{"t", "s", "time"},
+                              {"Ex", "V/m", "\"electric field\""},
+                              {"Ey", "V/m", "\"electric field\""},
+                              {"Ez", "V/m", "\"electric field\""},
+                              {"Bx", "T", "\"magnetic field\""},
+                              {"By", "T", "\"magnetic field\""},
+                              {"Bz", "T", "\"magnetic field\""}};
+    for (auto& c : cols)
+        std::fprintf(fp, "&column name=%s, symbol=%s, units=%s, description=%s, type=double, &end\n",
+                     c[0], c[0], c[1], c[2]);
+    std::fprintf(fp, "&data mode=ascii, &end\n");
+    std::fprintf(fp, "! page number 1\n");
+    std::fprintf(fp, "%zu\n%.17g\n%.17g\n", N, t0, dt);
+    std::fprintf(fp, "%zu\n", N);
+    for (std::size_t i = 0; i < N; i++) {
+        std::fprintf(fp, "%.17g", t0 + (double)i * dt);
+        for (int c = 0; c < 6; c++) std::fprintf(fp, " %.17g", f[6 * i + c]);
+        std::fprintf(fp, "\n");
+    }
+    if (std::fclose(fp) != 0)
+        throw IOexception("PointObserver::WriteTimeDomainFieldSDDS - error in Terminate()");
+}
+
+// One observation point (src/point_observer.cpp:30-110, 120-186).
 class PointObserver : public Observer<TrajectorySource> {
 public:
+    PointObserver(std::string filename, Vector position, double t0, double dt, std::size_t nots)
+        : FileName(std::move(filename)), Pos(position), trace(t0, dt, nots) {}
     PointObserver(Vector position, double t0, double dt, std::size_t nots)
         : Pos(position), trace(t0, dt, nots) {}
+    void WriteTimeDomainFieldSDDS() {
+        // B in Tesla: the C-ABI delivers the reference's getBuffer() layout
+        write_trace_sdds(FileName, trace.get_t0(), trace.get_dt(), trace.get_N(), trace.data());
+    }
+    void generateOutput() override { WriteTimeDomainFieldSDDS(); }
     void integrate() override {
         if (!source) throw IOexception("PointObserver::integrate - no source set");
         const double p[3] = {Pos.x, Pos.y, Pos.z};
@@ -276,6 +333,7 @@ public:
     }
 
 private:
+    std::string FileName;
     Vector Pos;
     FieldTrace trace;
 };

@@ -238,7 +238,8 @@ cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w
         lw_fp32_lanes_kernel<<<grid, 128, 0, s>>>(tr, sc, w);
         return cudaGetLastError();
     }
-    if (variant == kVariantPair) return launch_fp32_pair(tr, sc, w, s);
+    if (variant == kVariantPair || variant == kVariantPair3)
+        return launch_fp32_pair(tr, sc, w, variant, s);
     return launch_fp32_warp(tr, sc, w, variant, s);
 }
 

@@ -119,14 +119,21 @@ struct PointState2 {
     F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
 };
 
+// The anchors of both particles, as the loop uses them.
 struct Anchor2 {
-    Anchor a, b;
     V2 D;
     F2 err;
+    F2 frac;
+    int Ba, Bb;
 };
-__device__ __forceinline__ void pack_anchor(Anchor2& A) {
-    A.D = V2{f2(A.a.Dx, A.b.Dx), f2(A.a.Dy, A.b.Dy), f2(A.a.Dz, A.b.Dz)};
-    A.err = f2(A.a.err, A.b.err);
+__device__ __forceinline__ Anchor2 pack_anchor(const Anchor& a, const Anchor& b) {
+    Anchor2 A;
+    A.D = V2{f2(a.Dx, b.Dx), f2(a.Dy, b.Dy), f2(a.Dz, b.Dz)};
+    A.err = f2(a.err, b.err);
+    A.frac = f2(a.frac, b.frac);
+    A.Ba = a.Bi;
+    A.Bb = b.Bi;
+    return A;
 }
 
 // point_field (lw_fp32_point.cuh) for both particles at once.
@@ -192,10 +199,10 @@ __device__ __forceinline__ void chain_step2(const PointState2& p1, PointState2& 
 }
 
 __device__ __forceinline__ void start_chain2(PointState2& S, const Anchor2& A) {
-    const float kx = rintf(A.a.frac), ky = rintf(A.b.frac);
+    const float kx = rintf(A.frac.v.x), ky = rintf(A.frac.v.y);
     S.ka = (int)kx;
     S.kb = (int)ky;
-    S.r = f2(A.a.frac - kx, A.b.frac - ky);
+    S.r = A.frac - f2(kx, ky);
 }
 
 // One particle of a pair as a PointState, for the general deposit.
@@ -221,13 +228,11 @@ __device__ __forceinline__ PointState unpack(const PointState2& S) {
 struct PairSink {
     F2 acc[6];
     int open_a, open_b;
-    int nt;
     float* row;
     unsigned int err;
     unsigned int n_add;
-    __device__ void init(float* r, int n) {
+    __device__ void init(float* r) {
         row = r;
-        nt = n;
         open_a = open_b = -1;
         err = 0;
         n_add = 0;
@@ -259,7 +264,7 @@ struct PairSink {
     // The RedSink contract for particle W: f = component pairs (Ex,Ey),
     // (Ez,cBx), (cBy,cBz).
     template <int W>
-    __device__ __forceinline__ void add(int k, const float2* f) {
+    __device__ __forceinline__ void add(int k, const float2* f, int nt) {
         if (k < 0 || k >= nt) {
             err |= 1u << TEUFEL_ERR_RANGE;
             return;
@@ -319,7 +324,8 @@ struct PairSink {
 template <int W>
 struct PairView {
     PairSink* s;
-    __device__ __forceinline__ void add(int k, const float2* f) { s->add<W>(k, f); }
+    int nt;
+    __device__ __forceinline__ void add(int k, const float2* f) { s->add<W>(k, f, nt); }
 };
 
 // Regular steps of both particles (deposit_fast, lw_fp32_point.cuh, in packed
@@ -347,7 +353,7 @@ __device__ __forceinline__ void deposit_fast2(const PointState2& p1, const Point
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
-constexpr int kPThreads = 128;
+constexpr int kPThreads = 32;  // one warp per block: residency is set by registers alone
 constexpr int kPWarps = kPThreads / 32;
 
 // A staged chunk: p[0] is the pair-point before the chunk (the start of the
@@ -388,44 +394,57 @@ __device__ __forceinline__ int pair_of_segment(const int64_t* seg_offsets, int n
 // In-window step range of particle m within local steps [st_lo, st_hi), or
 // an empty range (first > last) when the lane has none.
 __device__ __forceinline__ void particle_range(const DevTraj& tr, int m, int st_lo, int st_hi,
-                                               bool active, const double3& P, const Window& w,
-                                               int& first, int& last) {
+                                               bool active, const PixelCtx& px, int& first,
+                                               int& last) {
     first = 0x7fffffff;
     last = -1;
     if (!active || st_lo >= st_hi) return;
     first = st_lo;
     last = st_hi - 1;
-    if (tr.vhat[m].w != 0.0) inwindow_steps(tr.tx + tr.offsets[m], st_lo, st_hi, P, w, &first, &last);
+    if (tr.vhat[m].w != 0.0)
+        inwindow_steps(tr.tx + tr.offsets[m], st_lo, st_hi, px.P, px.w, &first, &last);
     if (last < first) {
         first = 0x7fffffff;
         last = -1;
     }
 }
 
+// Warp-uniform parameters of the walk over one pair, kept in shared memory:
+// the inner loop reads them only at anchors.
+struct PairWalk {
+    const double4_32a* txa;
+    const double4_32a* txb;
+    const float4* pq;
+    int npa, npb, npp, n_pts;
+};
+
 template <int MINB>
 __global__ void __launch_bounds__(kPThreads, MINB)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
     __shared__ PairChunk buf[kPWarps][2];
     __shared__ PixelCtx pxs[kPThreads];
+    __shared__ PairWalk walks[kPWarps];
+    __shared__ unsigned long long stats[kPWarps][2];  // point evaluations, exact fallbacks
     const int slot = blockIdx.y;
     const int pix = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool active = pix < sc.np;
     const int pc = active ? pix : sc.np - 1;
-    const double3 P = make_double3(sc.pix_pos[3 * pc], sc.pix_pos[3 * pc + 1],
-                                   sc.pix_pos[3 * pc + 2]);
-    pxs[threadIdx.x] = make_pixel(P, sc.pix_t0[pc], sc.dt, sc.nt);
+    pxs[threadIdx.x] = make_pixel(make_double3(sc.pix_pos[3 * pc], sc.pix_pos[3 * pc + 1],
+                                               sc.pix_pos[3 * pc + 2]),
+                                  sc.pix_t0[pc], sc.dt, sc.nt);
+    if (lane == 0) stats[warp][0] = stats[warp][1] = 0;
     const PixelCtx& px = pxs[threadIdx.x];
-    const F2 kdt = f2(px.kdt, px.kdt);
     PairChunk* wb = buf[warp];
+    PairWalk& W = walks[warp];
     PairSink sink;
     sink.init(static_cast<float*>(wk.scratch) + (int64_t)slot * wk.slot_stride +
-                  (int64_t)pc * sc.nt * 6,
-              sc.nt);
-    const int nt = sc.nt;
+              (int64_t)pc * sc.nt * 6);
     const int64_t g0 = wk.slot_seg[slot], g1 = wk.slot_seg[slot + 1];
     int j = g0 < g1 ? pair_of_segment(tr.pair_seg_offsets, tr.n_pairs, g0) : tr.n_pairs;
-    unsigned long long inwin = 0, nfb = 0, nev = 0;
+    // a slot holds at most 2048 particles of at most 2^31 points: the
+    // per-thread deposit count stays below 2^32
+    unsigned int inwin = 0;
     for (; j < tr.n_pairs && tr.pair_seg_offsets[j] < g1; ++j) {
         const int64_t sb = tr.pair_seg_offsets[j];
         const int64_t se = tr.pair_seg_offsets[j + 1];
@@ -437,31 +456,40 @@ __global__ void __launch_bounds__(kPThreads, MINB)
         const int npa = (int)(tr.offsets[ma + 1] - tr.offsets[ma]);
         const int npb = hasb ? (int)(tr.offsets[mb + 1] - tr.offsets[mb]) : 0;
         const int st_lo = lg0 << kSegShift;
-        const int st_hi_a = min(lg1 << kSegShift, npa - 1);
-        const int st_hi_b = min(lg1 << kSegShift, npb - 1);
+        // the last point of a step of each particle in this slot (-1: none
+        // for this lane)
+        int lim_a = min(lg1 << kSegShift, npa - 1);
+        int lim_b = hasb ? min(lg1 << kSegShift, npb - 1) : -1;
         int fa, la, fb, lb;
-        particle_range(tr, ma, st_lo, st_hi_a, active, P, px.w, fa, la);
-        particle_range(tr, mb, st_lo, hasb ? st_hi_b : st_lo, active, P, px.w, fb, lb);
+        particle_range(tr, ma, st_lo, lim_a, active, px, fa, la);
+        particle_range(tr, mb, st_lo, hasb ? lim_b : st_lo, active, px, fb, lb);
+        if (!active) lim_a = lim_b = -1;
         const int lo = warp_min(min(fa, fb)), hi = warp_max(max(la, lb));
         if (lo > hi) continue;  // uniform over the warp
         const int start = lo & ~(kChunkLen - 1);  // >= st_lo, a segment boundary
-        const int n_pts = hi + 2 - start;           // points start .. hi+1
-        const int n_chunks = (n_pts + kChunkLen - 1) >> kChunkShift;
         const int64_t po = tr.pair_offsets[j];
-        const int npp = (int)(tr.pair_offsets[j + 1] - po);
-        const double4_32a* txa = tr.tx + tr.offsets[ma];
-        const double4_32a* txb = tr.tx + tr.offsets[mb];
-        const float4* pqj = tr.pq + 8 * po;
-        pair_stage(&wb[0], pqj, start, min(kChunkLen, npp - start), lane);
+        if (lane == 0) {
+            W.txa = tr.tx + tr.offsets[ma];
+            W.txb = tr.tx + tr.offsets[mb];
+            W.pq = tr.pq + 8 * po;
+            W.npa = npa;
+            W.npb = npb;
+            W.npp = (int)(tr.pair_offsets[j + 1] - po);
+            W.n_pts = hi + 2 - start;  // points start .. hi+1
+            stats[warp][0] += (unsigned long long)(hi + 2 - start) * (hasb ? 2u : 1u);
+        }
+        __syncwarp();
+        pair_stage(&wb[0], W.pq, start, min(kChunkLen, W.npp - start), lane);
         Anchor2 A;
         PointState2 p1, p2;
         F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);
         bool reg1a = false, reg1b = false;
+        const int n_chunks = (W.n_pts + kChunkLen - 1) >> kChunkShift;
         for (int c = 0; c < n_chunks; c++) {
             const int p0 = start + (c << kChunkShift);
             if (c + 1 < n_chunks) {
-                pair_stage(&wb[(c + 1) & 1], pqj, p0 + kChunkLen,
-                           min(kChunkLen, npp - (p0 + kChunkLen)), lane);
+                pair_stage(&wb[(c + 1) & 1], W.pq, p0 + kChunkLen,
+                           min(kChunkLen, W.npp - (p0 + kChunkLen)), lane);
                 asm volatile("cp.async.wait_group 1;\n" ::: "memory");
             } else {
                 asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -472,23 +500,24 @@ __global__ void __launch_bounds__(kPThreads, MINB)
                 c == 0 || (p0 & (kSegLen - 1)) == 0 ||
                 warp_any_above(fmaxf(chain_err.v.x, chain_err.v.y), kReanchorBound);
             if (anchor) {
-                Anchor2 An;
+                Anchor aa, ab;
                 // past its last point a particle repeats it, with positions
                 // relative to that point's segment; a particle without points
                 // borrows its partner's anchor (it never deposits)
-                const int ia = min(p0, npa - 1), ib = min(p0, npb - 1);
-                if (npa > 0) make_anchor(An.a, txa[ia], txa[ia & ~(kSegLen - 1)], px);
-                if (hasb && npb > 0) make_anchor(An.b, txb[ib], txb[ib & ~(kSegLen - 1)], px);
-                else An.b = An.a;
-                if (npa <= 0) An.a = An.b;
-                pack_anchor(An);
+                const int wa = W.npa, wbn = W.npb;
+                const int ia = min(p0, wa - 1), ib = min(p0, wbn - 1);
+                if (wa > 0) make_anchor(aa, W.txa[ia], W.txa[ia & ~(kSegLen - 1)], px);
+                if (wbn > 0) make_anchor(ab, W.txb[ib], W.txb[ib & ~(kSegLen - 1)], px);
+                else ab = aa;
+                if (wa <= 0) aa = ab;
+                const Anchor2 An = pack_anchor(aa, ab);
                 if (c > 0) {
-                    p1.ka += A.a.Bi - An.a.Bi;  // rebase: B + ki is unchanged
-                    p1.kb += A.b.Bi - An.b.Bi;
+                    p1.ka += A.Ba - An.Ba;  // rebase: B + ki is unchanged
+                    p1.kb += A.Bb - An.Bb;
                 }
                 A = An;
             }
-            const int n_here = min(kChunkLen, n_pts - (c << kChunkShift));
+            const int n_here = min(kChunkLen, W.n_pts - (c << kChunkShift));
             for (int l = 0; l < n_here; l++) {
                 const int i = p0 + l;
                 point_field2(p2, B.p[l + 1], A);
@@ -497,65 +526,67 @@ __global__ void __launch_bounds__(kPThreads, MINB)
                     comp = f2(0.0f, 0.0f);
                     chain_err = f2(0.0f, 0.0f);
                 } else {
-                    const F2 du = step_increment2(p1, p2, B.p[l], kdt);
+                    const F2 du = step_increment2(p1, p2, B.p[l], f2(px.kdt, px.kdt));
                     chain_step2(p1, p2, du, comp);
                     chain_err = fma(f2(fabsf(du.v.x), fabsf(du.v.y)),
                                     f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));
                 }
                 const F2 band = A.err + chain_err;
-                const bool dep_a = active && i > start && i <= st_hi_a;
-                const bool dep_b = active && hasb && i > start && i <= st_hi_b;
+                // the step ending at point i belongs to this lane and slot
+                const bool dep_a = i > start && i <= lim_a;
+                const bool dep_b = i > start && i <= lim_b;
+                const int nt = sc.nt;
                 bool reg2a, reg2b;
-                if (0.5f - fabsf(p2.r.v.x) <= band.v.x && i < npa) {
-                    const ExactPoint e = exact_point(txa, i, px, A.a.Bi);
+                if (0.5f - fabsf(p2.r.v.x) <= band.v.x && i <= lim_a) {
+                    const ExactPoint e = exact_point(W.txa, i, px, A.Ba);
                     p2.ka = e.ki;
                     p2.r.v.x = e.r;
                     p2.idxa = e.idx;
                     p2.fla = e.flags;
-                    nfb++;
+                    atomicAdd(&stats[warp][1], 1ull);
                     reg2a = false;
                 } else {
                     p2.fla = 0;
-                    reg2a = (unsigned)(A.a.Bi + p2.ka) < (unsigned)nt;
+                    reg2a = (unsigned)(A.Ba + p2.ka) < (unsigned)nt;
                 }
-                if (0.5f - fabsf(p2.r.v.y) <= band.v.y && hasb && i < npb) {
-                    const ExactPoint e = exact_point(txb, i, px, A.b.Bi);
+                if (0.5f - fabsf(p2.r.v.y) <= band.v.y && i <= lim_b) {
+                    const ExactPoint e = exact_point(W.txb, i, px, A.Bb);
                     p2.kb = e.ki;
                     p2.r.v.y = e.r;
                     p2.idxb = e.idx;
                     p2.flb = e.flags;
-                    nfb++;
+                    atomicAdd(&stats[warp][1], 1ull);
                     reg2b = false;
                 } else {
                     p2.flb = 0;
-                    reg2b = (unsigned)(A.b.Bi + p2.kb) < (unsigned)nt;
+                    reg2b = (unsigned)(A.Bb + p2.kb) < (unsigned)nt;
                 }
                 const bool fast_a = reg1a && reg2a && (unsigned)(p2.ka - p1.ka) <= 1u;
                 const bool fast_b = reg1b && reg2b && (unsigned)(p2.kb - p1.kb) <= 1u;
                 // steps that certainly lie outside the window: nothing to add
-                const bool out_a = (p2.fla == 0 && A.a.Bi + p2.ka < 0) ||
-                                   (!(p1.fla & kExact) && A.a.Bi + p1.ka >= nt);
-                const bool out_b = (p2.flb == 0 && A.b.Bi + p2.kb < 0) ||
-                                   (!(p1.flb & kExact) && A.b.Bi + p1.kb >= nt);
+                const bool out_a = (p2.fla == 0 && A.Ba + p2.ka < 0) ||
+                                   (!(p1.fla & kExact) && A.Ba + p1.ka >= nt);
+                const bool out_b = (p2.flb == 0 && A.Bb + p2.kb < 0) ||
+                                   (!(p1.flb & kExact) && A.Bb + p1.kb >= nt);
                 const bool ok = (!dep_a || fast_a || out_a) && (!dep_b || fast_b || out_b);
                 if (__all_sync(0xffffffffu, ok)) {
                     const bool da = dep_a && fast_a, db = dep_b && fast_b;
-                    if (da || db) deposit_fast2(p1, p2, A.a.Bi, A.b.Bi, da, db, sink);
+                    if (da || db) deposit_fast2(p1, p2, A.Ba, A.Bb, da, db, sink);
                     inwin += (unsigned)da + (unsigned)db;
                 } else {
                     if (dep_a) {
                         PointState q1 = unpack<0>(p1), q2 = unpack<0>(p2);
-                        materialize(q1, A.a.Bi, nt);
-                        materialize(q2, A.a.Bi, nt);
-                        PairView<0> v{&sink};
-                        if (deposit_step32(q1, q2, A.a.Bi, nt, v)) inwin++;
+                        materialize(q1, A.Ba, nt);
+                        materialize(q2, A.Ba, nt);
+                        PairView<0> v{&sink, nt};
+                        if (deposit_step32(q1, q2, A.Ba, nt, v)) inwin++;
                     }
                     if (dep_b) {
                         PointState q1 = unpack<1>(p1), q2 = unpack<1>(p2);
-                        materialize(q1, A.b.Bi, nt);
-                        materialize(q2, A.b.Bi, nt);
-                        PairView<1> v{&sink};
-                        if (deposit_step32(q1, q2, A.b.Bi, nt, v)) inwin++;
+                        materialize(q1, A.Bb, nt);
+                        materialize(q2, A.Bb, nt);
+                        PairView<1> v{&sink, nt};
+                        if (deposit_step32(q1, q2, A.Bb, nt, v)) inwin++;
                     }
                 }
                 reg1a = reg2a;
@@ -564,27 +595,28 @@ __global__ void __launch_bounds__(kPThreads, MINB)
             }
             __syncwarp();  // the buffer is restaged two chunks later
         }
-        if (active) nev += (unsigned long long)n_pts * (hasb ? 2u : 1u);
     }
     sink.flush<0>();
     sink.flush<1>();
     if (sink.err) atomicOr(wk.status, sink.err);
-    inwin = warp_sum_u64(active ? inwin : 0);
-    nfb = warp_sum_u64(active ? nfb : 0);
-    unsigned long long nadd = warp_sum_u64(sink.n_add);
-    nev = warp_sum_u64(nev);
+    const unsigned long long win = warp_sum_u64(inwin);
+    const unsigned long long nadd = warp_sum_u64(sink.n_add);
+    __syncwarp();
     if (lane == 0 && wk.counters) {
-        if (inwin) atomicAdd(wk.counters, inwin);
-        if (nfb) atomicAdd(wk.counters + 1, nfb);
+        if (win) atomicAdd(wk.counters, win);
+        if (stats[warp][1]) atomicAdd(wk.counters + 1, stats[warp][1]);
         if (nadd) atomicAdd(wk.counters + 2, nadd);
-        if (nev) atomicAdd(wk.counters + 3, nev);
+        if (stats[warp][0]) atomicAdd(wk.counters + 3, stats[warp][0]);
     }
 }
 
 cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
-                             cudaStream_t s) {
+                             int variant, cudaStream_t s) {
     dim3 grid((sc.np + kPThreads - 1) / kPThreads, w.n_slots);
-    lw_fp32_pair_kernel<3><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+    if (variant == kVariantPair3)
+        lw_fp32_pair_kernel<12><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+    else
+        lw_fp32_pair_kernel<16><<<grid, kPThreads, 0, s>>>(tr, sc, w);
     return cudaGetLastError();
 }
 

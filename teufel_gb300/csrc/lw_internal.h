@@ -90,7 +90,8 @@ namespace teufel {
 constexpr int kVariantUniform = 0;
 constexpr int kVariantLanes = 1;
 constexpr int kVariantWarp3 = 2;
-constexpr int kVariantPair = 3;  // two particles per thread, packed FP32 pairs
+constexpr int kVariantPair = 3;   // two particles per thread, packed FP32 pairs, 16 warps/SM
+constexpr int kVariantPair3 = 4;  // the same with registers sized for 12 warps/SM
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
@@ -110,7 +111,7 @@ cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const doubl
 cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s);
 cudaError_t launch_prep_pairs(const DevTraj& tr, cudaStream_t s);
 cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
-                             cudaStream_t s);
+                             int variant, cudaStream_t s);
 cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const double* ts,
                                       const double* f, double t0, double dt, int nt,
                                       double* trace, float* trace32, unsigned int* status,

@@ -138,8 +138,9 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     const int variant = opt.kernel_variant == 2   ? kVariantLanes
                         : opt.kernel_variant == 3 ? kVariantWarp3
                         : opt.kernel_variant == 4 ? kVariantPair
+                        : opt.kernel_variant == 5 ? kVariantPair3
                                                   : kVariantUniform;
-    const bool pairs = !fp64 && variant == kVariantPair;
+    const bool pairs = !fp64 && (variant == kVariantPair || variant == kVariantPair3);
     // work units: particle segments, or pair segments for the pair kernel
     const int64_t G = pairs ? h->dev.n_pair_segments : h->dev.n_segments;
     const int64_t units = pairs ? h->dev.n_pairs : h->dev.n_particles;
