@@ -62,11 +62,11 @@ typedef struct teufel_options {
     int precision;        /* TEUFEL_PREC_*                                        */
     int device_pointers;  /* 1: pix_pos, pix_t0 and out are device pointers      */
     int n_slots;          /* particle-range slots reduced in FP64; 0 = automatic  */
-    int kernel_variant;   /* FP32 path: 0 = automatic, 1 = warp-uniform steps,
-                             2 = per-pixel steps, 3 = warp-uniform steps with
-                             registers sized for 3 resident blocks per SM,
-                             4 = warp-uniform steps, two particles per thread,
-                             5 = the same with registers for 12 warps per SM  */
+    int kernel_variant;   /* FP32 path: 0 = automatic (4), 1 = warp-uniform
+                             steps, 2 = per-pixel steps, 3 = warp-uniform steps
+                             with registers for 3 blocks of 256 per SM,
+                             4/5/6/7 = warp-uniform steps, two particles per
+                             thread, 16/12/15/14 resident warps per SM        */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
 } teufel_options;
@@ -120,6 +120,67 @@ int teufel_cuda_integrate_point(const teufel_traj_set *traj, const double *pos, 
 int teufel_cuda_integrate_screen_ex(const teufel_traj_set *traj, const double *pix_pos,
                                     const double *pix_t0, double dt, int Nt, int Np, double *out,
                                     const teufel_options *opt, teufel_stream_t s);
+
+/* No counterpart in the reference.  Tunes the FP32 split-precision path for
+ * one observer shape: times the kernel variants (warp-uniform; two particles
+ * per thread at 12 to 16 resident warps per SM) at the automatic slot count,
+ * then the fastest at half and twice as many slots, on these very inputs,
+ * writing the trial traces to a scratch buffer (out-free: nothing is added
+ * anywhere).  *best receives *opt with kernel_variant and n_slots set to the
+ * winner, *best_ms (may be NULL) its time.  The choice is also remembered for
+ * the shape class -- the log2 sizes of Np, Nt, the particle count and the
+ * points per particle -- so later calls with kernel_variant = 0 on a similar
+ * shape use it.  opt->device_pointers says where pix_pos/pix_t0 live.
+ * Synchronous; runs the integration about nine times. */
+int teufel_cuda_autotune(const teufel_traj_set *traj, const double *pix_pos,
+                         const double *pix_t0, double dt, int Nt, int Np,
+                         const teufel_options *opt, teufel_options *best, double *best_ms);
+
+/* ---- batched observers ---------------------------------------------------- */
+
+/* One observer of a batch: its observation points and traces (the arguments
+ * of teufel_cuda_integrate_screen) and the trajectory set it integrates.
+ * Pointers are device pointers (a batch is planned once and then replayed). */
+typedef struct teufel_observer {
+    const teufel_traj_set *traj;
+    const double *pix_pos; /* [Np][3] */
+    const double *pix_t0;  /* [Np]    */
+    double dt;
+    int Nt;
+    int Np;
+    double *out;           /* [Np][Nt][6], added into */
+} teufel_observer;
+
+typedef struct teufel_batch teufel_batch;
+
+/* No single counterpart in the reference, whose driver integrates observer
+ * after observer (src/teufel_hybrid.cpp:692-709, each a call to
+ * BaseObserver::integrate).  Plans the FP32 split-precision integration of
+ * n_obs observers of uneven sizes -- mesh sizes, trace lengths, particle
+ * counts and trajectory lengths -- as ONE persistent kernel launch that takes
+ * (observer, pixel tile, particle range) work items from a device queue,
+ * largest first, followed by one reduction launch.  The plan (queue, slots,
+ * partial-trace memory) is built here; the launches are captured once into a
+ * CUDA graph, which teufel_cuda_batch_run replays.  Observers may share a
+ * trajectory set.  opt: precision must be TEUFEL_PREC_FP32_SPLIT;
+ * device_pointers must be 1; n_slots (0 = automatic) caps the particle
+ * ranges per observer.  The trajectory sets and device arrays must outlive
+ * the batch. */
+int teufel_cuda_batch_create(int n_obs, const teufel_observer *obs, const teufel_options *opt,
+                             teufel_batch **out);
+
+/* Run a planned batch on stream s: every observer's out is added into.
+ * Returns once the work is enqueued; the status of the run is returned by
+ * teufel_cuda_batch_status. */
+int teufel_cuda_batch_run(teufel_batch *batch, teufel_stream_t s);
+
+/* Synchronizes with the last run of the batch and returns its status
+ * (TEUFEL_ERR_RANGE when any deposit of any observer fell outside its
+ * trace).  Any pointer may be NULL. */
+int teufel_cuda_batch_status(teufel_batch *batch, int64_t *work_items, int64_t *inwindow,
+                             double *kernel_ms);
+
+int teufel_cuda_batch_free(teufel_batch *batch);
 
 /* ---- allocation-free integration ---------------------------------------- */
 

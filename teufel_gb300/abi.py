@@ -33,6 +33,8 @@ EXPORTED = [
     "teufel_cuda_integrate_point", "teufel_cuda_integrate_screen_ex",
     "teufel_cuda_point_decisions", "teufel_cuda_deposit_injected", "teufel_cuda_last_inwindow",
     "teufel_cuda_probe_peaks", "teufel_cuda_last_timing", "teufel_cuda_integrate_screen_noalloc",
+    "teufel_cuda_batch_create", "teufel_cuda_batch_run", "teufel_cuda_batch_status",
+    "teufel_cuda_batch_free", "teufel_cuda_autotune",
 ]
 
 # bytes of the fixed device array used by teufel_cuda_integrate_screen_noalloc
@@ -43,6 +45,13 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("n_slots", ctypes.c_int), ("kernel_variant", ctypes.c_int),
                 ("timing", ctypes.c_int)]
+
+
+class ObserverDesc(ctypes.Structure):
+    """teufel_observer: one observer of a batch (device pointers)."""
+    _fields_ = [("traj", ctypes.c_void_p), ("pix_pos", ctypes.c_void_p),
+                ("pix_t0", ctypes.c_void_p), ("dt", ctypes.c_double), ("Nt", ctypes.c_int),
+                ("Np", ctypes.c_int), ("out", ctypes.c_void_p)]
 
 
 class TeufelError(RuntimeError):
@@ -107,6 +116,20 @@ def lib():
                                                            ctypes.c_int, ctypes.c_int, _vp, _vp]
         L.teufel_cuda_probe_peaks.restype = ctypes.c_int
         L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp, _dp]
+        L.teufel_cuda_batch_create.restype = ctypes.c_int
+        L.teufel_cuda_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(ObserverDesc),
+                                               ctypes.POINTER(Options),
+                                               ctypes.POINTER(ctypes.c_void_p)]
+        L.teufel_cuda_batch_run.restype = ctypes.c_int
+        L.teufel_cuda_batch_run.argtypes = [_vp, _vp]
+        L.teufel_cuda_batch_status.restype = ctypes.c_int
+        L.teufel_cuda_batch_status.argtypes = [_vp, _lp, _lp, _dp]
+        L.teufel_cuda_autotune.restype = ctypes.c_int
+        L.teufel_cuda_autotune.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, ctypes.POINTER(Options),
+                                           ctypes.POINTER(Options), _dp]
+        L.teufel_cuda_batch_free.restype = ctypes.c_int
+        L.teufel_cuda_batch_free.argtypes = [_vp]
         _lib = L
     return _lib
 
@@ -248,6 +271,25 @@ class TrajSet:
               "teufel_cuda_last_timing")
         return int(dep.value), int(nev.value), int(nl.value), float(k.value), float(r.value)
 
+    def autotune(self, pix_pos, pix_t0, dt, nots, n_pix=None, device=False):
+        """teufel_cuda_autotune: (kernel_variant, n_slots, ms) of the fastest
+        FP32 configuration for this observer; later automatic calls on a
+        similar shape use it.  With device=True pix_pos/pix_t0 are device
+        pointers (ints) and n_pix must be given."""
+        opt = options(PREC_FP32_SPLIT, device)
+        best = Options()
+        ms = ctypes.c_double(0)
+        if device:
+            args = (ctypes.c_void_p(pix_pos), ctypes.c_void_p(pix_t0), dt, nots, int(n_pix))
+        else:
+            pos = _c(pix_pos).reshape(-1, 3)
+            t0 = _c(pix_t0).reshape(-1)
+            args = (pos.ctypes.data_as(ctypes.c_void_p), t0.ctypes.data_as(ctypes.c_void_p), dt,
+                    nots, pos.shape[0])
+        check(lib().teufel_cuda_autotune(self.handle, *args, ctypes.byref(opt), ctypes.byref(best),
+                                         ctypes.byref(ms)), "teufel_cuda_autotune")
+        return int(best.kernel_variant), int(best.n_slots), float(ms.value)
+
     def point_decisions(self, m, pos, t0, dt, nots):
         n = int(self.n_points[m])
         idx = np.zeros(n, dtype=np.int64)
@@ -285,3 +327,51 @@ def probe_peaks():
     check(lib().teufel_cuda_probe_peaks(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
           "probe_peaks")
     return a.value, b.value, c.value
+
+
+class Batch:
+    """A planned batch of observers (teufel_cuda_batch_create): one persistent
+    launch over a device work queue plus one reduction, replayed as a CUDA
+    graph.  observers: (TrajSet, pix_pos, pix_t0, dt, Nt, Np, out) with device
+    pointers (ints) for pix_pos, pix_t0 and out."""
+
+    def __init__(self, observers, n_slots: int = 0):
+        self._keep = [o[0] for o in observers]
+        arr = (ObserverDesc * max(1, len(observers)))()
+        for k, (ts, pos, t0, dt, nt, npix, out) in enumerate(observers):
+            arr[k] = ObserverDesc(ts.handle, pos, t0, dt, nt, npix, out)
+        opt = options(PREC_FP32_SPLIT, True, n_slots)
+        h = ctypes.c_void_p()
+        check(lib().teufel_cuda_batch_create(len(observers), arr, ctypes.byref(opt),
+                                             ctypes.byref(h)), "teufel_cuda_batch_create")
+        self.handle = h
+
+    def run(self, stream: int = 0) -> None:
+        check(lib().teufel_cuda_batch_run(self.handle, stream), "teufel_cuda_batch_run")
+
+    def status(self):
+        """(status, work items, in-window steps, integration-kernel ms) of the
+        last run; synchronizes with it."""
+        items = ctypes.c_int64(0)
+        inw = ctypes.c_int64(0)
+        ms = ctypes.c_double(0)
+        st = lib().teufel_cuda_batch_status(self.handle, ctypes.byref(items), ctypes.byref(inw),
+                                            ctypes.byref(ms))
+        return st, int(items.value), int(inw.value), float(ms.value)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().teufel_cuda_batch_free(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

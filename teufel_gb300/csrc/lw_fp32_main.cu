@@ -238,8 +238,7 @@ cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w
         lw_fp32_lanes_kernel<<<grid, 128, 0, s>>>(tr, sc, w);
         return cudaGetLastError();
     }
-    if (variant == kVariantPair || variant == kVariantPair3)
-        return launch_fp32_pair(tr, sc, w, variant, s);
+    if (is_pair_variant(variant)) return launch_fp32_pair(tr, sc, w, variant, s);
     return launch_fp32_warp(tr, sc, w, variant, s);
 }
 

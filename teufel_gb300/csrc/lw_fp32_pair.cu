@@ -115,6 +115,7 @@ struct PointState2 {
     F2 r;
     int idxa, idxb; // bin indices (general path only)
     int fla, flb;   // window flags; kExact when resolved exactly, else 0 until materialized
+    bool rega, regb;  // resolved without fallback, bin inside the trace
     V2 N;
     F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
 };
@@ -353,8 +354,7 @@ __device__ __forceinline__ void deposit_fast2(const PointState2& p1, const Point
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
-constexpr int kPThreads = 32;  // one warp per block: residency is set by registers alone
-constexpr int kPWarps = kPThreads / 32;
+constexpr int kPThreads = kPairTile;  // one warp per block: residency is set by registers alone
 
 // A staged chunk: p[0] is the pair-point before the chunk (the start of the
 // chunk's first step), p[1 + l] the chunk's point l.
@@ -418,25 +418,32 @@ struct PairWalk {
     int npa, npb, npp, n_pts;
 };
 
-template <int MINB>
-__global__ void __launch_bounds__(kPThreads, MINB)
-    lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
-    __shared__ PairChunk buf[kPWarps][2];
-    __shared__ PixelCtx pxs[kPThreads];
-    __shared__ PairWalk walks[kPWarps];
-    __shared__ unsigned long long stats[kPWarps][2];  // point evaluations, exact fallbacks
-    const int slot = blockIdx.y;
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const bool active = pix < sc.np;
-    const int pc = active ? pix : sc.np - 1;
-    pxs[threadIdx.x] = make_pixel(make_double3(sc.pix_pos[3 * pc], sc.pix_pos[3 * pc + 1],
-                                               sc.pix_pos[3 * pc + 2]),
-                                  sc.pix_t0[pc], sc.dt, sc.nt);
-    if (lane == 0) stats[warp][0] = stats[warp][1] = 0;
-    const PixelCtx& px = pxs[threadIdx.x];
-    PairChunk* wb = buf[warp];
-    PairWalk& W = walks[warp];
+// Shared memory of one block (one warp).
+struct PairShared {
+    PairChunk buf[2];
+    PixelCtx px[kPThreads];
+    PairWalk walk;
+    unsigned long long stats[2];  // point evaluations, exact fallbacks
+};
+
+// One pixel tile (kPThreads pixels of the observer) against one slot of the
+// trajectory set: the whole work of a block of the per-observer kernel, and
+// one work item of the batched kernel.
+__device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
+                                          const DevWork& wk, int slot, int tile,
+                                          PairShared& sh) {
+    const int pix = tile * kPThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int np = sc.np;
+    const bool active = pix < np;
+    const int pc = active ? pix : np - 1;
+    sh.px[threadIdx.x] = make_pixel(make_double3(sc.pix_pos[3 * pc], sc.pix_pos[3 * pc + 1],
+                                                 sc.pix_pos[3 * pc + 2]),
+                                    sc.pix_t0[pc], sc.dt, sc.nt);
+    if (lane == 0) sh.stats[0] = sh.stats[1] = 0;
+    const PixelCtx& px = sh.px[threadIdx.x];
+    PairChunk* wb = sh.buf;
+    PairWalk& W = sh.walk;
     PairSink sink;
     sink.init(static_cast<float*>(wk.scratch) + (int64_t)slot * wk.slot_stride +
               (int64_t)pc * sc.nt * 6);
@@ -476,14 +483,14 @@ __global__ void __launch_bounds__(kPThreads, MINB)
             W.npb = npb;
             W.npp = (int)(tr.pair_offsets[j + 1] - po);
             W.n_pts = hi + 2 - start;  // points start .. hi+1
-            stats[warp][0] += (unsigned long long)(hi + 2 - start) * (hasb ? 2u : 1u);
+            sh.stats[0] += (unsigned long long)(hi + 2 - start) * (hasb ? 2u : 1u);
         }
         __syncwarp();
         pair_stage(&wb[0], W.pq, start, min(kChunkLen, W.npp - start), lane);
         Anchor2 A;
         PointState2 p1, p2;
-        F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);
-        bool reg1a = false, reg1b = false;
+        F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);  // chain_err includes A.err
+        p2.rega = p2.regb = false;
         const int n_chunks = (W.n_pts + kChunkLen - 1) >> kChunkShift;
         for (int c = 0; c < n_chunks; c++) {
             const int p0 = start + (c << kChunkShift);
@@ -512,86 +519,93 @@ __global__ void __launch_bounds__(kPThreads, MINB)
                 if (wa <= 0) aa = ab;
                 const Anchor2 An = pack_anchor(aa, ab);
                 if (c > 0) {
-                    p1.ka += A.Ba - An.Ba;  // rebase: B + ki is unchanged
-                    p1.kb += A.Bb - An.Bb;
+                    // rebase the chunk's previous point (in p2, see below):
+                    // B + ki is unchanged
+                    p2.ka += A.Ba - An.Ba;
+                    p2.kb += A.Bb - An.Bb;
                 }
                 A = An;
             }
             const int n_here = min(kChunkLen, W.n_pts - (c << kChunkShift));
-            for (int l = 0; l < n_here; l++) {
+            // One step: point l of the chunk into q2, deposit q1 -> q2.  The
+            // loop below alternates the roles of p1 and p2, so the point
+            // state is never copied.
+            auto step = [&](PointState2& q1, PointState2& q2, int l) {
                 const int i = p0 + l;
-                point_field2(p2, B.p[l + 1], A);
+                point_field2(q2, B.p[l + 1], A);
                 if (l == 0 && anchor) {
-                    start_chain2(p2, A);
+                    start_chain2(q2, A);
                     comp = f2(0.0f, 0.0f);
-                    chain_err = f2(0.0f, 0.0f);
+                    chain_err = A.err;
                 } else {
-                    const F2 du = step_increment2(p1, p2, B.p[l], f2(px.kdt, px.kdt));
-                    chain_step2(p1, p2, du, comp);
+                    const F2 du = step_increment2(q1, q2, B.p[l], f2(px.kdt, px.kdt));
+                    chain_step2(q1, q2, du, comp);
                     chain_err = fma(f2(fabsf(du.v.x), fabsf(du.v.y)),
                                     f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));
                 }
-                const F2 band = A.err + chain_err;
                 // the step ending at point i belongs to this lane and slot
                 const bool dep_a = i > start && i <= lim_a;
                 const bool dep_b = i > start && i <= lim_b;
                 const int nt = sc.nt;
-                bool reg2a, reg2b;
-                if (0.5f - fabsf(p2.r.v.x) <= band.v.x && i <= lim_a) {
+                if (0.5f - fabsf(q2.r.v.x) <= chain_err.v.x && i <= lim_a) {
                     const ExactPoint e = exact_point(W.txa, i, px, A.Ba);
-                    p2.ka = e.ki;
-                    p2.r.v.x = e.r;
-                    p2.idxa = e.idx;
-                    p2.fla = e.flags;
-                    atomicAdd(&stats[warp][1], 1ull);
-                    reg2a = false;
+                    q2.ka = e.ki;
+                    q2.r.v.x = e.r;
+                    q2.idxa = e.idx;
+                    q2.fla = e.flags;
+                    atomicAdd(&sh.stats[1], 1ull);
+                    q2.rega = false;
                 } else {
-                    p2.fla = 0;
-                    reg2a = (unsigned)(A.Ba + p2.ka) < (unsigned)nt;
+                    q2.fla = 0;
+                    q2.rega = (unsigned)(A.Ba + q2.ka) < (unsigned)nt;
                 }
-                if (0.5f - fabsf(p2.r.v.y) <= band.v.y && i <= lim_b) {
+                if (0.5f - fabsf(q2.r.v.y) <= chain_err.v.y && i <= lim_b) {
                     const ExactPoint e = exact_point(W.txb, i, px, A.Bb);
-                    p2.kb = e.ki;
-                    p2.r.v.y = e.r;
-                    p2.idxb = e.idx;
-                    p2.flb = e.flags;
-                    atomicAdd(&stats[warp][1], 1ull);
-                    reg2b = false;
+                    q2.kb = e.ki;
+                    q2.r.v.y = e.r;
+                    q2.idxb = e.idx;
+                    q2.flb = e.flags;
+                    atomicAdd(&sh.stats[1], 1ull);
+                    q2.regb = false;
                 } else {
-                    p2.flb = 0;
-                    reg2b = (unsigned)(A.Bb + p2.kb) < (unsigned)nt;
+                    q2.flb = 0;
+                    q2.regb = (unsigned)(A.Bb + q2.kb) < (unsigned)nt;
                 }
-                const bool fast_a = reg1a && reg2a && (unsigned)(p2.ka - p1.ka) <= 1u;
-                const bool fast_b = reg1b && reg2b && (unsigned)(p2.kb - p1.kb) <= 1u;
+                const bool fast_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= 1u;
+                const bool fast_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= 1u;
                 // steps that certainly lie outside the window: nothing to add
-                const bool out_a = (p2.fla == 0 && A.Ba + p2.ka < 0) ||
-                                   (!(p1.fla & kExact) && A.Ba + p1.ka >= nt);
-                const bool out_b = (p2.flb == 0 && A.Bb + p2.kb < 0) ||
-                                   (!(p1.flb & kExact) && A.Bb + p1.kb >= nt);
+                const bool out_a = (q2.fla == 0 && A.Ba + q2.ka < 0) ||
+                                   (!(q1.fla & kExact) && A.Ba + q1.ka >= nt);
+                const bool out_b = (q2.flb == 0 && A.Bb + q2.kb < 0) ||
+                                   (!(q1.flb & kExact) && A.Bb + q1.kb >= nt);
                 const bool ok = (!dep_a || fast_a || out_a) && (!dep_b || fast_b || out_b);
                 if (__all_sync(0xffffffffu, ok)) {
                     const bool da = dep_a && fast_a, db = dep_b && fast_b;
-                    if (da || db) deposit_fast2(p1, p2, A.Ba, A.Bb, da, db, sink);
+                    if (da || db) deposit_fast2(q1, q2, A.Ba, A.Bb, da, db, sink);
                     inwin += (unsigned)da + (unsigned)db;
                 } else {
                     if (dep_a) {
-                        PointState q1 = unpack<0>(p1), q2 = unpack<0>(p2);
-                        materialize(q1, A.Ba, nt);
-                        materialize(q2, A.Ba, nt);
+                        PointState u1 = unpack<0>(q1), u2 = unpack<0>(q2);
+                        materialize(u1, A.Ba, nt);
+                        materialize(u2, A.Ba, nt);
                         PairView<0> v{&sink, nt};
-                        if (deposit_step32(q1, q2, A.Ba, nt, v)) inwin++;
+                        if (deposit_step32(u1, u2, A.Ba, nt, v)) inwin++;
                     }
                     if (dep_b) {
-                        PointState q1 = unpack<1>(p1), q2 = unpack<1>(p2);
-                        materialize(q1, A.Bb, nt);
-                        materialize(q2, A.Bb, nt);
+                        PointState u1 = unpack<1>(q1), u2 = unpack<1>(q2);
+                        materialize(u1, A.Bb, nt);
+                        materialize(u2, A.Bb, nt);
                         PairView<1> v{&sink, nt};
-                        if (deposit_step32(q1, q2, A.Bb, nt, v)) inwin++;
+                        if (deposit_step32(u1, u2, A.Bb, nt, v)) inwin++;
                     }
                 }
-                reg1a = reg2a;
-                reg1b = reg2b;
-                p1 = p2;
+            };
+            // chunks are kChunkLen (even) points long, so point l of every
+            // chunk lives in p1 for even l and in p2 for odd l, and the point
+            // before a chunk in p2
+            for (int l = 0; l < n_here; l += 2) {
+                step(p2, p1, l);
+                if (l + 1 < n_here) step(p1, p2, l + 1);
             }
             __syncwarp();  // the buffer is restaged two chunks later
         }
@@ -604,19 +618,62 @@ __global__ void __launch_bounds__(kPThreads, MINB)
     __syncwarp();
     if (lane == 0 && wk.counters) {
         if (win) atomicAdd(wk.counters, win);
-        if (stats[warp][1]) atomicAdd(wk.counters + 1, stats[warp][1]);
+        if (sh.stats[1]) atomicAdd(wk.counters + 1, sh.stats[1]);
         if (nadd) atomicAdd(wk.counters + 2, nadd);
-        if (stats[warp][0]) atomicAdd(wk.counters + 3, stats[warp][0]);
+        if (sh.stats[0]) atomicAdd(wk.counters + 3, sh.stats[0]);
     }
 }
+
+// MAXREG: the register budget per thread, which sets how many one-warp
+// blocks are resident per SM (65536 / (32 MAXREG)): 128 -> 16, 136 -> 15,
+// 144 -> 14, 160 -> 12.  Below the natural ~158 the compiler spills a little.
+template <int MAXREG>
+__global__ void __maxnreg__(MAXREG)
+    lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
+    __shared__ PairShared sh;
+    pair_tile(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
+}
+
+// Persistent form: every block takes (observer, tile, slot) items from the
+// queue until it is empty.
+template <int MAXREG>
+__global__ void __maxnreg__(MAXREG)
+    lw_fp32_pair_batch_kernel(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
+                              const BatchItem* items, int n_items, unsigned int* head) {
+    __shared__ PairShared sh;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned int it = 0;
+        if (lane == 0) it = atomicAdd(head, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= (unsigned int)n_items) break;
+        const BatchItem bi = items[it];
+        pair_tile(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile, sh);
+        __syncwarp();
+    }
+}
+
 
 cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
                              int variant, cudaStream_t s) {
     dim3 grid((sc.np + kPThreads - 1) / kPThreads, w.n_slots);
-    if (variant == kVariantPair3)
-        lw_fp32_pair_kernel<12><<<grid, kPThreads, 0, s>>>(tr, sc, w);
-    else
-        lw_fp32_pair_kernel<16><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+    switch (variant) {
+        case kVariantPair160: lw_fp32_pair_kernel<160><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
+        case kVariantPair136: lw_fp32_pair_kernel<136><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
+        case kVariantPair144: lw_fp32_pair_kernel<144><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
+        default: lw_fp32_pair_kernel<128><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
+    }
+    return cudaGetLastError();
+}
+
+constexpr int kBatchMaxReg = 144;
+int pair_batch_blocks_per_sm() { return 65536 / (32 * kBatchMaxReg); }
+
+cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
+                                   const BatchItem* items, int n_items, unsigned int* head,
+                                   int n_blocks, cudaStream_t s) {
+    lw_fp32_pair_batch_kernel<kBatchMaxReg><<<n_blocks, kPThreads, 0, s>>>(trs, scs, wks, items,
+                                                                          n_items, head);
     return cudaGetLastError();
 }
 

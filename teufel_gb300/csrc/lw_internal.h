@@ -90,8 +90,14 @@ namespace teufel {
 constexpr int kVariantUniform = 0;
 constexpr int kVariantLanes = 1;
 constexpr int kVariantWarp3 = 2;
-constexpr int kVariantPair = 3;   // two particles per thread, packed FP32 pairs, 16 warps/SM
-constexpr int kVariantPair3 = 4;  // the same with registers sized for 12 warps/SM
+// two particles per thread, packed FP32 pairs, one-warp blocks, with a
+// register budget of 128 / 160 / 136 / 144 per thread (16 / 12 / 15 / 14
+// resident warps per SM)
+constexpr int kVariantPair = 3;
+constexpr int kVariantPair160 = 4;
+constexpr int kVariantPair136 = 5;
+constexpr int kVariantPair144 = 6;
+constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPair144; }
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
@@ -117,4 +123,27 @@ cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const dou
                                       double* trace, float* trace32, unsigned int* status,
                                       cudaStream_t s);
 int probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops);
+
+// One work item of a batched launch: a pixel tile of an observer against one
+// slot (particle range) of its trajectory set.
+struct BatchItem {
+    int obs;
+    int tile;
+    int slot;
+};
+// The persistent batched kernel (pair kernel body) and the batched reduction.
+cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
+                                   const BatchItem* items, int n_items, unsigned int* head,
+                                   int n_blocks, cudaStream_t s);
+int pair_batch_blocks_per_sm();
+constexpr int kPairTile = 32;  // pixels per tile of the pair kernel
+cudaError_t launch_reduce_fp32_batch(const DevWork* wks, const DevScreen* scs,
+                                     double* const* outs, const int64_t* bin_prefix, int n_obs,
+                                     int64_t n_bins, cudaStream_t s);
+}  // namespace teufel
+
+struct teufel_traj_set;
+namespace teufel {
+// device view and status word of a trajectory handle (teufel_abi.cu)
+const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** status);
 }  // namespace teufel

@@ -82,12 +82,6 @@ int fail(cudaError_t e) {
 
 }  // namespace
 
-// Access to the trajectory handle's device view; defined with the handle in
-// teufel_abi.cu.
-namespace teufel {
-const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** status);
-}
-
 extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
                                                     const double* d_pix_pos,
                                                     const double* d_pix_t0, double dt, int Nt,

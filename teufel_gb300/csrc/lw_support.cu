@@ -10,10 +10,11 @@ namespace teufel {
 // out[p][k][c] += sum over slots (in slot order, FP64) of the partial
 // traces; the partial slots are cleared for the next call.  The FP32 path
 // stores c*B, so the B components are divided by c here.
-__global__ void reduce_fp32_kernel(DevWork w, int64_t n_bins, double* out) {
+// out[e] += the sum over slots of the FP32 partial traces of bin e (B from
+// cB), and the partial traces cleared for the next use.
+__device__ __forceinline__ void reduce_fp32_bin(const DevWork& w, int64_t e, double* out) {
     const float* scr = static_cast<const float*>(w.scratch);
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
-         e += (int64_t)gridDim.x * blockDim.x) {
+    {
         double acc[6] = {0, 0, 0, 0, 0, 0};
         // all loads first (independent, so they overlap), then the clears
         for (int s = 0; s < w.n_slots; s++) {
@@ -40,6 +41,27 @@ __global__ void reduce_fp32_kernel(DevWork w, int64_t n_bins, double* out) {
         o[3] += acc[3] / kC;
         o[4] += acc[4] / kC;
         o[5] += acc[5] / kC;
+    }
+}
+
+__global__ void reduce_fp32_kernel(DevWork w, int64_t n_bins, double* out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
+         e += (int64_t)gridDim.x * blockDim.x)
+        reduce_fp32_bin(w, e, out);
+}
+
+// All observers of a batch: bin e of the concatenation belongs to the last
+// observer o with prefix[o] <= e.
+__global__ void reduce_fp32_batch_kernel(const DevWork* wks, double* const* outs,
+                                         const int64_t* prefix, int n_obs, int64_t n_bins) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_obs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= e) lo = mid; else hi = mid - 1;
+        }
+        reduce_fp32_bin(wks[lo], e - prefix[lo], outs[lo]);
     }
 }
 
@@ -81,6 +103,16 @@ cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* ou
     int64_t n = (int64_t)sc.np * sc.nt;
     if (n == 0) return cudaSuccess;
     reduce_fp32_kernel<<<reduce_blocks(n), 256, 0, s>>>(w, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_fp32_batch(const DevWork* wks, const DevScreen* scs,
+                                     double* const* outs, const int64_t* bin_prefix, int n_obs,
+                                     int64_t n_bins, cudaStream_t s) {
+    (void)scs;
+    if (n_bins == 0) return cudaSuccess;
+    reduce_fp32_batch_kernel<<<reduce_blocks(n_bins), 256, 0, s>>>(wks, outs, bin_prefix, n_obs,
+                                                                   n_bins);
     return cudaGetLastError();
 }
 

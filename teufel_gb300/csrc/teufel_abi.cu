@@ -10,7 +10,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "lw_internal.h"
@@ -40,6 +43,7 @@ struct teufel_traj_set {
     int last_launches = 0;
     bool last_timed = false;
     std::vector<int64_t> h_seg_offsets;
+    int last_slots = 0;
 };
 
 namespace {
@@ -132,15 +136,56 @@ bool finite_array(const double* p, int64_t n) {
 
 // Device part of an integration: partial traces per slot, then the FP64
 // reduction into out (device pointers).  Enqueued on s.
+// ---- tuned choices per shape class (teufel_cuda_autotune) ----
+struct TuneKey {
+    int np, nt, parts, pts;  // log2 buckets of pixels, samples, particles, points/particle
+    bool operator<(const TuneKey& o) const {
+        return std::tie(np, nt, parts, pts) < std::tie(o.np, o.nt, o.parts, o.pts);
+    }
+};
+struct TuneChoice {
+    int variant;      // kernel_variant
+    int slot_pct;     // slot count relative to the automatic one [%]
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneChoice> g_tuned;
+
+int log2_bucket(int64_t v) {
+    int b = 0;
+    while (v > 1) {
+        v >>= 1;
+        b++;
+    }
+    return b;
+}
+TuneKey tune_key(const teufel_traj_set* h, int np, int nt) {
+    const int64_t n = std::max<int64_t>(h->dev.n_particles, 1);
+    return TuneKey{log2_bucket(np), log2_bucket(nt), log2_bucket(n),
+                   log2_bucket(h->dev.n_points / n)};
+}
+
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
-               int np, double* d_out, const teufel_options& opt, cudaStream_t s) {
+               int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
+               int slot_pct = 100) {
+    teufel_options opt = opt_in;
     const bool fp64 = opt.precision == TEUFEL_PREC_FP64;
-    const int variant = opt.kernel_variant == 2   ? kVariantLanes
+    if (!fp64 && opt.kernel_variant == 0) {
+        // automatic: a tuned choice for this shape class, if there is one
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(tune_key(h, np, nt));
+        if (it != g_tuned.end()) {
+            opt.kernel_variant = it->second.variant;
+            if (opt.n_slots <= 0) slot_pct = it->second.slot_pct;
+        }
+    }
+    const int variant = opt.kernel_variant == 1   ? kVariantUniform
+                        : opt.kernel_variant == 2 ? kVariantLanes
                         : opt.kernel_variant == 3 ? kVariantWarp3
-                        : opt.kernel_variant == 4 ? kVariantPair
-                        : opt.kernel_variant == 5 ? kVariantPair3
-                                                  : kVariantUniform;
-    const bool pairs = !fp64 && (variant == kVariantPair || variant == kVariantPair3);
+                        : opt.kernel_variant == 5 ? kVariantPair160
+                        : opt.kernel_variant == 6 ? kVariantPair136
+                        : opt.kernel_variant == 7 ? kVariantPair144
+                                                  : kVariantPair;  // 0 (automatic), 4
+    const bool pairs = !fp64 && is_pair_variant(variant);
     // work units: particle segments, or pair segments for the pair kernel
     const int64_t G = pairs ? h->dev.n_pair_segments : h->dev.n_segments;
     const int64_t units = pairs ? h->dev.n_pairs : h->dev.n_particles;
@@ -152,6 +197,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     int64_t target = opt.n_slots > 0 ? opt.n_slots
                                      : (152LL * 512 * 4 + (int64_t)pix_blocks * kThreads - 1) /
                                            ((int64_t)pix_blocks * kThreads);
+    if (opt.n_slots <= 0) target = std::max<int64_t>(1, target * slot_pct / 100);
     int64_t slots_total = std::max<int64_t>(target, 1);
     if (!fp64 && opt.n_slots <= 0)
         slots_total = std::max<int64_t>(slots_total,
@@ -164,6 +210,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     per_pass = std::max<int64_t>(1, std::min<int64_t>(per_pass, slots_total));
     int rc = grow(&h->scratch, &h->scratch_bytes, slot_bytes * (size_t)per_pass, true);
     if (rc) return rc;
+    h->last_slots = (int)slots_total;
     std::vector<int64_t> bounds(slots_total + 1);
     for (int64_t k = 0; k <= slots_total; k++) bounds[k] = G * k / slots_total;
     if (h->slot_cap < slots_total + 1) {
@@ -432,6 +479,95 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     }
     TRY_CUDA(cudaMemcpyAsync(out, h->d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
     return finish(h, s);
+}
+
+int teufel_cuda_autotune(const teufel_traj_set* traj_c, const double* pix_pos,
+                         const double* pix_t0, double dt, int Nt, int Np,
+                         const teufel_options* opt_in, teufel_options* best, double* best_ms) {
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj_c);
+    if (!best || !valid_screen_args(h, pix_pos, pix_t0, dt, Nt, Np, pix_pos)) return TEUFEL_ERR_ARG;
+    teufel_options opt;
+    teufel_cuda_default_options(&opt);
+    if (opt_in) opt = *opt_in;
+    if (opt.precision != TEUFEL_PREC_FP32_SPLIT) return TEUFEL_ERR_ARG;
+    *best = opt;
+    if (best_ms) *best_ms = 0.0;
+    if (Nt < 2 || Np == 0 || h->dev.n_particles == 0 || h->dev.n_segments == 0) return TEUFEL_OK;
+    if (!(dt > 0.0) && !(dt < 0.0)) return TEUFEL_ERR_ARG;
+    cudaStream_t s = nullptr;
+    TRY_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    double* d_pix = nullptr;
+    double* d_scr = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&](int rc) {
+        if (s) cudaStreamSynchronize(s);
+        if (d_pix) cudaFree(d_pix);
+        if (d_scr) cudaFree(d_scr);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (s) cudaStreamDestroy(s);
+        return rc;
+    };
+    const double* d_pos = pix_pos;
+    const double* d_t0 = pix_t0;
+    if (!opt.device_pointers) {
+        if (!finite_array(pix_pos, 3 * (int64_t)Np) || !finite_array(pix_t0, Np))
+            return cleanup(TEUFEL_ERR_ARG);
+        if (cudaMalloc(&d_pix, sizeof(double) * 4 * (size_t)Np) != cudaSuccess ||
+            cudaMemcpy(d_pix, pix_pos, sizeof(double) * 3 * Np, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(d_pix + 3 * (size_t)Np, pix_t0, sizeof(double) * Np, cudaMemcpyHostToDevice))
+            return cleanup(cuda_fail(cudaGetLastError()));
+        d_pos = d_pix;
+        d_t0 = d_pix + 3 * (size_t)Np;
+    }
+    // the traces of the trial runs go to a scratch buffer, never to the caller's
+    if (cudaMalloc(&d_scr, sizeof(double) * 6 * (size_t)Np * (size_t)Nt) != cudaSuccess ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return cleanup(cuda_fail(cudaGetLastError()));
+    opt.device_pointers = 1;
+    opt.timing = 0;
+    auto trial = [&](int variant, int pct, float* ms) {
+        teufel_options o = opt;
+        o.kernel_variant = variant;
+        if (cudaEventRecord(e0, s) != cudaSuccess) return cuda_fail(cudaGetLastError());
+        int rc = run_device(h, d_pos, d_t0, dt, Nt, Np, d_scr, o, s, pct);
+        if (rc) return rc;
+        if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)
+            return cuda_fail(cudaGetLastError());
+        return TEUFEL_OK;
+    };
+    // variants at the automatic slot count, then the best one at half and
+    // twice as many slots; the first trial also loads the modules
+    const int variants[] = {4, 7, 6, 5, 1};
+    float ms = 0.0f, best_t = 1e30f;
+    int bv = 4, bp = 100, rc;
+    if ((rc = trial(4, 100, &ms))) return cleanup(rc);
+    for (int v : variants) {
+        if ((rc = trial(v, 100, &ms))) return cleanup(rc);
+        if (ms < best_t) {
+            best_t = ms;
+            bv = v;
+        }
+    }
+    for (int pct : {50, 200}) {
+        if ((rc = trial(bv, pct, &ms))) return cleanup(rc);
+        if (ms < best_t) {
+            best_t = ms;
+            bp = pct;
+        }
+    }
+    // the slot count the choice resolves to, for callers that pass it explicitly
+    if ((rc = trial(bv, bp, &ms))) return cleanup(rc);
+    best->kernel_variant = bv;
+    best->n_slots = h->last_slots;
+    if (best_ms) *best_ms = best_t;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tuned[tune_key(h, Np, Nt)] = TuneChoice{bv, bp};
+    }
+    for (auto& c : h->last_counters) c = 0;
+    return cleanup(TEUFEL_OK);
 }
 
 int teufel_cuda_integrate_screen(const teufel_traj_set* traj, const double* pix_pos,
