@@ -57,6 +57,10 @@ def parse():
                     help="trace samples (0 = the workload's 4096); only for small profiling runs")
     ap.add_argument("--variant", type=int, default=0,
                     help="FP32 kernel variant (teufel_options.kernel_variant; 0 = automatic)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (the automatic variant then uses its default)")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched-observer measurement")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -140,6 +144,57 @@ def make_batches(n_batches, batch, nthreads=0):
         first = (b * batch) % 100000
         out.append(H.config4(first=first, count=batch, nthreads=nthreads))
     return out
+
+
+KERNEL_NAMES = {0: "lw_fp32_pair_kernel<128>", 1: "lw_fp32_warp_kernel<2>",
+                2: "lw_fp32_lanes_kernel", 3: "lw_fp32_warp_kernel<3>",
+                4: "lw_fp32_pair_kernel<128>", 5: "lw_fp32_pair_kernel<160>",
+                6: "lw_fp32_pair_kernel<136>", 7: "lw_fp32_pair_kernel<144>"}
+
+
+def batch_measure(dev, reps=2, scale=64):
+    """The batched uneven observers (16 seeded screens of the batched-observer
+    configuration, each screen's particle draw divided by `scale`) as one
+    teufel_cuda_batch: evaluations per second of one graph replay."""
+    import torch
+    from teufel_gb300 import abi, harness as H
+    sets, bufs, obs = [], [], []
+    evals = 0
+    for spec in H.config3_specs():
+        w = H.config3_screen(spec, count=max(4, spec["n_particles"] // scale))
+        ts = abi.TrajSet(w.traj)
+        pos = torch.from_numpy(np.ascontiguousarray(w.pix_pos)).to(dev)
+        t0 = torch.from_numpy(np.ascontiguousarray(w.pix_t0)).to(dev)
+        out = torch.zeros((w.n_pix, w.nots, 6), dtype=torch.float64, device=dev)
+        sets.append(ts)
+        bufs.append((pos, t0, out))
+        obs.append((ts, pos.data_ptr(), t0.data_ptr(), w.dt, w.nots, w.n_pix, out.data_ptr()))
+        evals += w.n_pix * int(np.sum(w.traj.n_points - 1))
+    b = abi.Batch(obs)
+    b.run()
+    st, items, _, _ = b.status()
+    abi.check(st, "batch")
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        b.run(torch.cuda.current_stream(dev).cuda_stream)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    st, items, inwin, kms = b.status()
+    abi.check(st, "batch")
+    b.close()
+    for ts in sets:
+        ts.free()
+    return {"value": evals / (best / 1e3), "unit": UNIT, "observers": len(obs),
+            "work_items": items, "evals": evals, "ms": best,
+            "launches": "one persistent integration kernel + one reduction, replayed as a CUDA graph",
+            "workload": f"16 seeded screens of the batched uneven-observer configuration "
+                        f"(meshes 16^2..128^2, 512..8192 samples, 2e3..2e4 steps), each with "
+                        f"its particle draw / {scale} (min 4)"}
 
 
 def shard(n, rank, world):
@@ -250,6 +305,15 @@ def run_gb300(args):
     sets = [abi.TrajSet(b.traj) for b in batches]
     evals_step = n_pix * args.batch * (npts - 1)
 
+    # the autotuner times the kernel configurations on the first batch; the
+    # automatic variant (0) then uses its choice for this shape
+    tuned = None
+    if args.variant == 0 and not args.no_tune:
+        tv, tslots, tms = sets[0].autotune(pos.data_ptr(), t0.data_ptr(), w0.dt, nots,
+                                           n_pix=n_pix, device=True)
+        tuned = {"kernel_variant": tv, "n_slots": tslots, "ms": tms}
+        torch.cuda.synchronize(dev)
+
     def step(j, timing):
         sets[j % n_batches].integrate_screen_device(pos.data_ptr(), t0.data_ptr(), w0.dt, nots,
                                                     n_pix, out.data_ptr(), stream=sptr,
@@ -346,6 +410,16 @@ def run_gb300(args):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": 1e3 * float(el_all.item()) / K}
 
+    batch = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        # the trajectory sets of the timed loop are released first
+        for ts in sets:
+            ts.free()
+        sets = []
+        out = None
+        torch.cuda.empty_cache()
+        batch = batch_measure(dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -375,13 +449,16 @@ def run_gb300(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": TRAFFIC_PER_LAUNCH,
-                         "kernel": "lw_fp32_warp_kernel",
+                         "kernel": KERNEL_NAMES.get(tuned["kernel_variant"] if tuned
+                                                    else args.variant, "?"),
                          "peak_source": "the larger of the FFMA and packed-FFMA2 throughput "
                                         "probes run by bench.py on this GPU "
                                         "(MEASURED_PEAKS.json has no FP32 figure)",
                          "ffma_probe_tflops": peak32, "ffma2_probe_tflops": peak32x2,
                          "algorithmic_flops": flops, "kernel_ms": kernel_ms,
                          "reduce_ms": reduce_ms, "fp64_probe_tflops": peak64},
+            "autotune": tuned,
+            "batched_observers": batch,
             "gpu_launches": launches,
             "clocks": clk,
             "e2e": e2e,

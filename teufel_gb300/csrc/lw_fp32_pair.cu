@@ -429,6 +429,7 @@ struct PairShared {
 // One pixel tile (kPThreads pixels of the observer) against one slot of the
 // trajectory set: the whole work of a block of the per-observer kernel, and
 // one work item of the batched kernel.
+template <bool PINGPONG>
 __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
                                           const DevWork& wk, int slot, int tile,
                                           PairShared& sh) {
@@ -600,12 +601,21 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                     }
                 }
             };
-            // chunks are kChunkLen (even) points long, so point l of every
-            // chunk lives in p1 for even l and in p2 for odd l, and the point
-            // before a chunk in p2
-            for (int l = 0; l < n_here; l += 2) {
-                step(p2, p1, l);
-                if (l + 1 < n_here) step(p1, p2, l + 1);
+            if (PINGPONG) {
+                // chunks are kChunkLen (even) points long, so point l of every
+                // chunk lives in p1 for even l and in p2 for odd l, and the
+                // point before a chunk in p2
+                for (int l = 0; l < n_here; l += 2) {
+                    step(p2, p1, l);
+                    if (l + 1 < n_here) step(p1, p2, l + 1);
+                }
+            } else {
+                // one copy of the step body (fewer registers), the new point
+                // copied into place after each step
+                for (int l = 0; l < n_here; l++) {
+                    step(p2, p1, l);
+                    p2 = p1;
+                }
             }
             __syncwarp();  // the buffer is restaged two chunks later
         }
@@ -626,12 +636,14 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 
 // MAXREG: the register budget per thread, which sets how many one-warp
 // blocks are resident per SM (65536 / (32 MAXREG)): 128 -> 16, 136 -> 15,
-// 144 -> 14, 160 -> 12.  Below the natural ~158 the compiler spills a little.
-template <int MAXREG>
+// 144 -> 14, 160 -> 13 (the unrolled loop needs ~152).  PINGPONG: the inner
+// loop unrolled by two with alternating point states (no copies, more
+// registers) or one step body with a copy per step.
+template <int MAXREG, bool PINGPONG>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
     __shared__ PairShared sh;
-    pair_tile(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
+    pair_tile<PINGPONG>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
 }
 
 // Persistent form: every block takes (observer, tile, slot) items from the
@@ -648,7 +660,7 @@ __global__ void __maxnreg__(MAXREG)
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= (unsigned int)n_items) break;
         const BatchItem bi = items[it];
-        pair_tile(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile, sh);
+        pair_tile<false>(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile, sh);
         __syncwarp();
     }
 }
@@ -658,15 +670,23 @@ cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWo
                              int variant, cudaStream_t s) {
     dim3 grid((sc.np + kPThreads - 1) / kPThreads, w.n_slots);
     switch (variant) {
-        case kVariantPair160: lw_fp32_pair_kernel<160><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
-        case kVariantPair136: lw_fp32_pair_kernel<136><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
-        case kVariantPair144: lw_fp32_pair_kernel<144><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
-        default: lw_fp32_pair_kernel<128><<<grid, kPThreads, 0, s>>>(tr, sc, w); break;
+        case kVariantPair160:
+            lw_fp32_pair_kernel<160, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+            break;
+        case kVariantPair136:
+            lw_fp32_pair_kernel<136, false><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+            break;
+        case kVariantPair144:
+            lw_fp32_pair_kernel<144, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+            break;
+        default:
+            lw_fp32_pair_kernel<128, false><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+            break;
     }
     return cudaGetLastError();
 }
 
-constexpr int kBatchMaxReg = 144;
+constexpr int kBatchMaxReg = 128;
 int pair_batch_blocks_per_sm() { return 65536 / (32 * kBatchMaxReg); }
 
 cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
