@@ -360,3 +360,138 @@ void lwo_step_decisions(int64_t np, const double *t, const double *x, const doub
         else kase[s] = 2;
     }
 }
+
+/* ---------------------------------------------------------------------------
+ * The field at one observation time and place:
+ *   ChargedParticle::RetardedField(double obs_time, Vector obs_pos)
+ *                                               src/particle.cpp:612-769
+ *   Bunch::RetardedField (sum in particle order)    src/bunch.cpp:729-737
+ * -------------------------------------------------------------------------*/
+
+/* The LW field of a source at SourceX moving with SourceBeta (gamma2 =
+   gamma^2) and d(beta)/dt = betap, observed at o (src/particle.cpp:750-766). */
+static void field_of_source(v3 o, v3 sx, v3 beta, v3 betap, double gamma2, double charge,
+                            double *out6)
+{
+    v3 rv = v3_sub(o, sx);
+    double R = v3_norm(rv);
+    v3 n = rv;
+    double nn = v3_norm(n);
+    n.x /= nn; n.y /= nn; n.z /= nn;
+    double scale = charge * LWO_E_CHARGE / (4.0 * LWO_PI * LWO_EPS0);
+    double k3 = pow(1.0 - v3_dot(beta, n), 3.0);
+    v3 E = v3_div(v3_sub(n, beta), R * R * k3 * gamma2);
+    v3 acc = v3_cross(n, v3_cross(v3_sub(n, beta), betap));
+    E = v3_add(E, v3_div(acc, R * k3 * LWO_C));
+    E = v3_mul(E, scale);
+    v3 B = v3_div(v3_cross(n, E), LWO_C);
+    out6[0] = E.x; out6[1] = E.y; out6[2] = E.z;
+    out6[3] = B.x; out6[4] = B.y; out6[5] = B.z;
+}
+
+/* One particle of np points (np >= 1).  Adds its field into acc6. */
+static void retarded_field_particle(int64_t np, const double *T, const double *Xa,
+                                    const double *Pa, const double *Aa, double charge,
+                                    double obs_time, v3 o, double *acc6)
+{
+#define PT(a, i) ((v3){(a)[3 * (i)], (a)[3 * (i) + 1], (a)[3 * (i) + 2]})
+    int64_t i1 = 0, i2 = np - 1;
+    double R1 = v3_norm(v3_sub(o, PT(Xa, i1)));
+    double t1 = obs_time - (T[i1] + R1 / LWO_C);
+    double R2 = v3_norm(v3_sub(o, PT(Xa, i2)));
+    double t2 = obs_time - (T[i2] + R2 / LWO_C);
+    if (!(t2 <= 0.0)) return; /* no signal has arrived yet */
+    v3 sx, beta, betap;
+    double gamma2;
+    if (t1 <= 0.0) {
+        /* extrapolation to negative trajectory times (src/particle.cpp:639-659) */
+        v3 Rc = v3_div(v3_sub(o, PT(Xa, 0)), LWO_C);
+        beta = PT(Pa, 0);
+        double bg2 = v3_abs2(beta);
+        gamma2 = bg2 + 1.0;
+        double gamma = sqrt(gamma2);
+        beta = v3_div(beta, gamma);
+        double t0 = obs_time;
+        double bR = v3_dot(beta, Rc);
+        double bb = v3_dot(beta, beta);
+        double RR = v3_dot(Rc, Rc);
+        double st = (t0 - bR - sqrt((t0 - bR) * (t0 - bR) - (1 - bb) * (t0 * t0 - RR))) / (1 - bb);
+        sx = v3_add(PT(Xa, 0), v3_mul(v3_mul(beta, LWO_C), st));
+        betap = (v3){0.0, 0.0, 0.0};
+    } else {
+        /* bisection to a single step (src/particle.cpp:666-685) */
+        while (i2 - i1 > 1) {
+            int64_t im = (i2 + i1) / 2;
+            double Rm = v3_norm(v3_sub(o, PT(Xa, im)));
+            double tm = obs_time - (T[im] + Rm / LWO_C);
+            if (tm > 0.0) { i1 = im; t1 = tm; }
+            else { i2 = im; t2 = tm; }
+        }
+        double frac = t1 / (t1 - t2);
+        /* secant refinement (src/particle.cpp:693-733) */
+        double tt1 = T[i1], tt2 = T[i2];
+        v3 X1 = PT(Xa, i1), X2 = PT(Xa, i2);
+        double st = tt1 * (1.0 - frac) + tt2 * frac;
+        sx = v3_add(v3_mul(X1, 1.0 - frac), v3_mul(X2, frac));
+        double R = v3_norm(v3_sub(o, sx));
+        double dt = st + R / LWO_C - obs_time;
+        double r1 = v3_norm(v3_sub(o, X1));
+        double r2 = v3_norm(v3_sub(o, X2));
+        double dtdfrac = (tt2 - tt1) + (r2 - r1) / LWO_C;
+        double dfrac = dt / dtdfrac;
+        int nref = 1;
+        while (fabs(dfrac) > 1e-5 && nref < 10) {
+            double last = dt;
+            frac -= dfrac;
+            st = tt1 * (1.0 - frac) + tt2 * frac;
+            sx = v3_add(v3_mul(X1, 1.0 - frac), v3_mul(X2, frac));
+            R = v3_norm(v3_sub(o, sx));
+            dt = st + R / LWO_C - obs_time;
+            dtdfrac = -(dt - last) / dfrac;
+            dfrac = dt / dtdfrac;
+            nref++;
+        }
+        frac -= dfrac;
+        sx = v3_add(v3_mul(X1, 1.0 - frac), v3_mul(X2, frac));
+        beta = v3_add(v3_mul(PT(Pa, i1), 1.0 - frac), v3_mul(PT(Pa, i2), frac));
+        double bg2 = v3_abs2(beta);
+        gamma2 = bg2 + 1.0;
+        double gamma = sqrt(gamma2);
+        beta = v3_div(beta, gamma);
+        betap = v3_add(v3_mul(PT(Aa, i1), 1.0 - frac), v3_mul(PT(Aa, i2), frac));
+        betap = v3_div(betap, gamma);
+    }
+    double f[6];
+    field_of_source(o, sx, beta, betap, gamma2, charge, f);
+    for (int k = 0; k < 6; k++) acc6[k] += f[k];
+#undef PT
+}
+
+/* The summed field of all particles (charges in units of e) at obs_time on
+   each of np observation points: out[np][6] is overwritten, as
+   SnapshotObserver::integrate assigns (src/snapshot.cpp:72-80).  Returns
+   LWO_ERR_RANGE if a particle has no trajectory point, where the reference
+   throws RANGEexception (src/particle.cpp:615). */
+int lwo_retarded_field_at(int64_t n_part, const int64_t *offsets, const double *charge,
+                          const double *t, const double *x, const double *bg, const double *a,
+                          double obs_time, int64_t np, const double *pos, double *out,
+                          int nthreads)
+{
+    for (int64_t m = 0; m < n_part; m++)
+        if (offsets[m + 1] - offsets[m] < 1) return LWO_ERR_RANGE;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t p = 0; p < np; p++) {
+        v3 o = {pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int64_t m = 0; m < n_part; m++) {
+            int64_t b = offsets[m];
+            retarded_field_particle(offsets[m + 1] - b, t + b, x + 3 * b, bg + 3 * b, a + 3 * b,
+                                    charge[m], obs_time, o, acc);
+        }
+        for (int k = 0; k < 6; k++) out[6 * p + k] = acc[k];
+    }
+    return LWO_OK;
+}

@@ -476,6 +476,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         if (lo > hi) continue;  // uniform over the warp
         const int start = lo & ~(kChunkLen - 1);  // >= st_lo, a segment boundary
         const int64_t po = tr.pair_offsets[j];
+        const unsigned int lanes = __popc(__ballot_sync(0xffffffffu, active));
         if (lane == 0) {
             W.txa = tr.tx + tr.offsets[ma];
             W.txb = tr.tx + tr.offsets[mb];
@@ -484,7 +485,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             W.npb = npb;
             W.npp = (int)(tr.pair_offsets[j + 1] - po);
             W.n_pts = hi + 2 - start;  // points start .. hi+1
-            sh.stats[0] += (unsigned long long)(hi + 2 - start) * (hasb ? 2u : 1u);
+            sh.stats[0] += (unsigned long long)(hi + 2 - start) * (hasb ? 2u : 1u) * lanes;
         }
         __syncwarp();
         pair_stage(&wb[0], W.pq, start, min(kChunkLen, W.npp - start), lane);
