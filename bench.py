@@ -37,9 +37,10 @@ UNIT = "evals/s"
 # of a multi-bin step (one LW field evaluation 89 + single-bin deposit 21)
 FLOPS_PER_STEP = 110.0
 FLOPS_PER_EXTRA_BIN = 14.0
-# dram bytes per launch of lw_fp32_kernel at the default batch, from the ncu
-# capture summarised in profiles/lw_fp32_kernel_config4.md (None until measured)
-TRAFFIC_PER_LAUNCH = None
+# DRAM bytes (read + write) per in-window (pixel, particle, step) of the pair
+# kernel, from one ncu capture of a 5000-pixel, 32-particle, 2048-sample case:
+# 2.401e9 B / 2.475e8 in-window steps
+DRAM_BYTES_PER_INWINDOW_STEP = 9.70
 
 
 def parse():
@@ -448,7 +449,10 @@ def run_gb300(args):
                          "sample": f"{len(sub)} pixels x {args.batch} particles"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
-                         "traffic": TRAFFIC_PER_LAUNCH,
+                         "traffic": DRAM_BYTES_PER_INWINDOW_STEP * inwin / max(K, 1),
+                         "traffic_note": "DRAM bytes per launch: ncu's 9.70 B per in-window "
+                                         "step on a small case, times the in-window steps of "
+                                         "one launch (an estimate)",
                          "kernel": KERNEL_NAMES.get(tuned["kernel_variant"] if tuned
                                                     else args.variant, "?"),
                          "peak_source": "the larger of the FFMA and packed-FFMA2 throughput "

@@ -121,6 +121,21 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set *traj, const double *p
                                     const double *pix_t0, double dt, int Nt, int Np, double *out,
                                     const teufel_options *opt, teufel_stream_t s);
 
+/* The summed field of all particles at time obs_time on Np points: replaces
+ * SnapshotObserver<Beam>::integrate (src/snapshot.cpp:72-80), i.e.
+ * Beam/Bunch::RetardedField(double, Vector) (src/beam.cpp:433-441,
+ * src/bunch.cpp:729-737) at every point.  pos[Np][3] (host); out[Np][6]
+ * (host, Ex,Ey,Ez,Bx,By,Bz) is overwritten, as the snapshot assigns.  FP64 with
+ * the reference's algorithm (src/particle.cpp:612-769): a particle contributes
+ * nothing where the signal of its last trajectory point has not arrived yet;
+ * before its first point it is extrapolated backwards at constant velocity;
+ * otherwise the emission point is found by bisection of the trajectory and
+ * secant refinement inside the step.  A particle
+ * without trajectory points returns TEUFEL_ERR_RANGE (the reference throws
+ * RANGEexception).  Synchronous. */
+int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int Np,
+                               const double *pos, double *out, teufel_stream_t s);
+
 /* No counterpart in the reference.  Tunes the FP32 split-precision path for
  * one observer shape: times the kernel variants (warp-uniform; two particles
  * per thread at 12 to 16 resident warps per SM) at the automatic slot count,

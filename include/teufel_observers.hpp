@@ -338,4 +338,64 @@ private:
     FieldTrace trace;
 };
 
+// The field of the source on an Nx x Ny grid at one time
+// (src/snapshot.cpp:30-80, 405-408): cell (ix, iy) observes at
+// O + dX (ix - (Nx-1)/2) + dY (iy - (Ny-1)/2) at time t; integrate() assigns
+// the summed retarded field of all particles through
+// teufel_cuda_retarded_field.
+class SnapshotObserver : public Observer<TrajectorySource> {
+public:
+    SnapshotObserver(std::string filename, Vector position, Vector dx, Vector dy, unsigned int nx,
+                     unsigned int ny, double t)
+        : FileName(std::move(filename)), O(position), dX(dx), dY(dy), Nx(nx), Ny(ny), t_obs(t),
+          buf(6 * (std::size_t)nx * ny, 0.0) {}
+    Vector CellPosition(int ix, int iy) const {
+        return O + dX * ((double)ix - 0.5 * ((double)Nx - 1.0)) +
+               dY * ((double)iy - 0.5 * ((double)Ny - 1.0));
+    }
+    void integrate() override {
+        if (!source) throw IOexception("SnapshotObserver::integrate - no source set");
+        std::vector<double> pos(3 * (std::size_t)Nx * Ny);
+        for (unsigned int ix = 0; ix < Nx; ix++)
+            for (unsigned int iy = 0; iy < Ny; iy++) {
+                const Vector p = CellPosition((int)ix, (int)iy);
+                double* q = pos.data() + 3 * ((std::size_t)ix * Ny + iy);
+                q[0] = p.x;
+                q[1] = p.y;
+                q[2] = p.z;
+            }
+        check_status(teufel_cuda_retarded_field(source->device(), t_obs, (int)(Nx * Ny),
+                                                pos.data(), buf.data(), nullptr),
+                     "SnapshotObserver::integrate");
+    }
+    ElMagField getField(unsigned int ix, unsigned int iy) const {
+        ElMagField f;
+        std::memcpy(f.c, buf.data() + 6 * ((std::size_t)ix * Ny + iy), sizeof f.c);
+        return f;
+    }
+    std::size_t getBufferSize() override { return buf.size(); }
+    double* getBuffer() override {
+        double* b = new double[buf.size()];
+        if (!buf.empty()) std::memcpy(b, buf.data(), sizeof(double) * buf.size());
+        return b;
+    }
+    void fromBuffer(double* buffer, std::size_t size) override {
+        if (size != buf.size())
+            throw IOexception("SnapshotObserver::fromBuffer() - buffer size mismatch.");
+        if (size) std::memcpy(buf.data(), buffer, sizeof(double) * size);
+    }
+    // The reference writes HDF5 here (src/snapshot.cpp); this build has no
+    // HDF5 library, so the fields leave through getBuffer().
+    void generateOutput() override {
+        throw IOexception("SnapshotObserver::generateOutput - HDF5 output is not available in this build");
+    }
+
+private:
+    std::string FileName;
+    Vector O, dX, dY;
+    unsigned int Nx, Ny;
+    double t_obs;
+    std::vector<double> buf;  // [Nx][Ny][6]
+};
+
 }  // namespace teufel_gb300

@@ -65,6 +65,9 @@ def oracle():
         L.lwo_point_decisions.restype = None
         L.lwo_point_decisions.argtypes = [_i64, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                           _i64, _lp, ctypes.POINTER(ctypes.c_int32)]
+        L.lwo_retarded_field_at.restype = ctypes.c_int
+        L.lwo_retarded_field_at.argtypes = [_i64, _lp, _dp, _dp, _dp, _dp, _dp, ctypes.c_double,
+                                            _i64, _dp, _dp, ctypes.c_int]
         L.lwo_step_decisions.restype = None
         L.lwo_step_decisions.argtypes = [_i64, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                          _i64, _lp, _lp, _bp]
@@ -84,6 +87,9 @@ def reference():
         L.ref_integrate_screen.restype = ctypes.c_int
         L.ref_integrate_screen.argtypes = [_i64, _lp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _dp,
                                            _dp, ctypes.c_double, _i64, _dp, ctypes.c_int]
+        L.ref_retarded_field_at.restype = ctypes.c_int
+        L.ref_retarded_field_at.argtypes = [_i64, _lp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                            ctypes.c_double, _i64, _dp, _dp]
         L.ref_deposit_injected.restype = ctypes.c_int
         L.ref_deposit_injected.argtypes = [_i64, _lp, _dp, _dp, ctypes.c_double,
                                            ctypes.c_double, _i64, _dp]
@@ -136,6 +142,29 @@ def deposit_injected(ts_list, f_list, t0, dt, nots, impl="oracle"):
     fn = oracle().lwo_deposit_injected if impl == "oracle" else reference().ref_deposit_injected
     rc = fn(len(ts_list), _p(offs, _lp), _p(ts), _p(f), t0, dt, nots, _p(trace))
     return trace, rc
+
+
+def retarded_field_at(traj, obs_time, pos, nthreads=0, impl="oracle"):
+    """The summed field [n_obs, 6] of a particle set at time obs_time on the
+    observation points pos[n_obs, 3] (ChargedParticle::RetardedField(double,
+    Vector) per particle, summed as Bunch::RetardedField).  impl: "oracle" or
+    "reference"."""
+    pos = _c(pos).reshape(-1, 3)
+    n = pos.shape[0]
+    out = np.zeros((n, 6))
+    offs = _c(traj.offsets, np.int64)
+    t, x, p, a = _c(traj.t), _c(traj.x), _c(traj.p), _c(traj.a)
+    ch = _c(traj.charge)
+    if impl == "oracle":
+        rc = oracle().lwo_retarded_field_at(traj.n_particles, _p(offs, _lp), _p(ch), _p(t), _p(x),
+                                            _p(p), _p(a), ctypes.c_double(obs_time), n, _p(pos),
+                                            _p(out), nthreads)
+    else:
+        ms = _c(traj.mass)
+        rc = reference().ref_retarded_field_at(traj.n_particles, _p(offs, _lp), _p(ch), _p(ms),
+                                               _p(t), _p(x), _p(p), _p(a),
+                                               ctypes.c_double(obs_time), n, _p(pos), _p(out))
+    return out, rc
 
 
 def point_decisions(traj, m, obs, t0, dt, nots):

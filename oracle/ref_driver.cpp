@@ -168,6 +168,48 @@ int ref_integrate_screen(int64_t n_part, const int64_t* offsets, const double* c
     return err;
 }
 
+// The reference's ChargedParticle::RetardedField(double, Vector) summed over
+// the particles in order as Bunch::RetardedField does (src/bunch.cpp:729-737),
+// on np observation points at obs_time; out[np][6] is overwritten.
+int ref_retarded_field_at(int64_t n_part, const int64_t* offsets, const double* charge,
+                          const double* mass, const double* t, const double* x, const double* p,
+                          const double* a, double obs_time, int64_t n_obs, const double* pos,
+                          double* out) {
+    std::vector<ChargedParticle*> parts;
+    parts.reserve(n_part);
+    for (int64_t m = 0; m < n_part; m++) {
+        int64_t o = offsets[m], np = offsets[m + 1] - o;
+        std::vector<double> buf(9 + 10 * np, 0.0);
+        buf[0] = charge[m];
+        buf[1] = mass[m];
+        for (int64_t k = 0; k < np; k++) {
+            double* b = buf.data() + 9 + 10 * k;
+            b[0] = t[o + k];
+            std::memcpy(b + 1, x + 3 * (o + k), 24);
+            std::memcpy(b + 4, p + 3 * (o + k), 24);
+            std::memcpy(b + 7, a + 3 * (o + k), 24);
+        }
+        parts.push_back(new ChargedParticle(buf.data(), (int)np, 0));
+    }
+    int err = 0;
+    for (int64_t ip = 0; ip < n_obs && !err; ip++) {
+        const double* pp = pos + 3 * ip;
+        ElMagField f;
+        try {
+            for (int64_t m = 0; m < n_part; m++)
+                f += parts[m]->RetardedField(obs_time, Vector(pp[0], pp[1], pp[2]));
+        } catch (...) {
+            err = 4;
+        }
+        Vector E = f.E(), B = f.B();
+        double* o = out + 6 * ip;
+        o[0] = E.x; o[1] = E.y; o[2] = E.z;
+        o[3] = B.x; o[4] = B.y; o[5] = B.z;
+    }
+    for (auto* q : parts) delete q;
+    return err;
+}
+
 int ref_deposit_injected(int64_t n_part, const int64_t* offsets, const double* ts,
                          const double* f, double t0, double dt, int64_t nots, double* trace) {
     FieldTrace tr(t0, dt, (std::size_t)nots);

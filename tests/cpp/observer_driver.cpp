@@ -1,12 +1,14 @@
 // Exercises the C++ observer layer (include/teufel_observers.hpp) on the GPU:
 // reads trajectories and an observer description from a binary file written
 // by tests/test_gpu_observers.py, runs ScreenObserver, MeshedScreen and
-// PointObserver integrate(), and writes their getBuffer() contents.
+// PointObserver integrate() and a SnapshotObserver on the same grid at the
+// middle of the trace window, and writes their getBuffer() contents.
 //
 // input  (doubles unless noted): int32 n_part; int32 npts[n]; charge[n];
 //        t[N]; x[N*3]; p[N*3]; a[N*3];
 //        origin[3], dx[3], dy[3], int32 nx, int32 ny, t0, dt, dtx, dty, int32 nots
-// output: screen buffer [nx*ny*nots*6], mesh buffer (same pixels), point buffer [nots*6]
+// output: screen buffer [nx*ny*nots*6], mesh buffer (same pixels), point buffer [nots*6],
+//         snapshot buffer [nx*ny*6]
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -93,6 +95,14 @@ int main(int argc, char** argv) {
         PointObserver tiny(pts[c], tz[c], dt, 1);
         tiny.setSource(&beam);
         tiny.integrate();
+        // the field on the same grid at the middle of the trace window
+        SnapshotObserver snap("", Vector(o[0], o[1], o[2]), Vector(dx[0], dx[1], dx[2]),
+                              Vector(dy[0], dy[1], dy[2]), nx, ny, t0 + 0.5 * nots * dt);
+        snap.setSource(&beam);
+        snap.integrate();
+        b = snap.getBuffer();
+        fwrite(b, sizeof(double), snap.getBufferSize(), out);
+        delete[] b;
     } catch (const IOexception& e) {
         fprintf(stderr, "IOexception: %s\n", e.what());
         fclose(out);

@@ -16,6 +16,11 @@ Fixtures (numpy .npz, compressed):
   screen_bunch.npz    the same for the four-particle bunch on 8 pixels
   range_error.npz     injected arrival times for which FieldTrace::add throws
                       (src/fieldtrace.cpp:185-190) inside the reference
+  retarded_field.npz  ChargedParticle::RetardedField(double, Vector)
+                      (src/particle.cpp:612-769) of the reference's
+                      electrostatic test (tests/teufel.electrostatic.cpp:60-233:
+                      a 1 pC charge at rest, and moving at gamma = 10 through a
+                      field-free region) and of the single-electron undulator run
 """
 import os
 import sys
@@ -142,11 +147,65 @@ def range_errors():
                         status=np.array(status), traces=np.array(traces))
 
 
+def electrostatic_cases():
+    """The scenario of tests/teufel.electrostatic.cpp:60-233: trajectories
+    and observation (time, points) sets."""
+    q = -1.0e-12 / E_CHARGE
+    rest = H.Trajectories(np.zeros(1), np.zeros((1, 3)), np.zeros((1, 3)), np.zeros((1, 3)),
+                          np.array([1], np.int32), np.array([q]), np.array([1.0]))
+    gamma = 10.0
+    bg = np.sqrt(gamma * gamma - 1.0)
+    d = np.array([2.0, 3.0, 5.0])
+    d = d / np.sqrt(np.sum(d * d))
+    perp = np.cross(d, [1.0, 0.0, 0.0])
+    perp = perp / np.sqrt(np.sum(perp * perp))
+    n_steps, tau = 2000, 4.0e-9
+    init = np.array([[0.0, 0.0, 0.0, 0.0, bg * d[0], bg * d[1], bg * d[2]]])
+    lat = H.Lattice(hom_b=(0.0, 0.0, 0.0))
+    t, x, p, a = lw.track_reference(init, lat.packed(), tau / n_steps, n_steps, q, 1.0)
+    moving = H.Trajectories(t, x, p, a, np.array([n_steps + 1], np.int32), np.array([q]),
+                            np.array([1.0]))
+    beta = np.sqrt(1.0 - 1.0 / (gamma * gamma))
+    ls = -0.005 + 0.001 * np.arange(11)
+    p0 = perp * 0.001
+    p1 = d * 3.0e-9 * beta * C + perp * 0.001
+    sets = [
+        ("rest", rest, 0.0, np.array([[0.001, 0.0, 0.0], [-0.001, 0.0, 0.0], [0.0, 0.0, 0.001]])),
+        ("moving_t0", moving, 0.0, np.vstack([p0] + [p0 + d * l for l in ls])),
+        ("moving_t3ns", moving, 3.0e-9, np.vstack([p1] + [p1 + d * l for l in ls])),
+    ]
+    return sets, dict(d=d, perp=perp, gamma=gamma, beta=beta)
+
+
+def retarded_fields(tr1):
+    sets, geo = electrostatic_cases()
+    w = H.config1()
+    traj1 = H.Trajectories(tr1[0], tr1[1], tr1[2], tr1[3], np.array([len(tr1[0])], np.int32),
+                           np.array([-1.0]), np.array([1.0]))
+    pos = w.pix_pos[::29]
+    for k, tobs in enumerate((0.0, 2.0e-8, 3.34e-8, 3.4e-8, 3.5e-8, 1.0e-6)):
+        sets.append((f"undulator_{k}", traj1, tobs, pos))
+    rec, trajs = {}, {}
+    for name, tr, tobs, p in sets:
+        out, rc = lw.retarded_field_at(tr, tobs, p, impl="reference")
+        assert rc == 0
+        key = name.split("_")[0]
+        trajs[key] = tr
+        rec[name] = dict(traj=key, obs_time=tobs, pos=p, fields=out)
+    flat = {f"{n}__{k}": v for n, d in rec.items() for k, v in d.items()}
+    for key, tr in trajs.items():
+        for f in ("t", "x", "p", "a", "n_points", "charge", "mass"):
+            flat[f"traj_{key}__{f}"] = getattr(tr, f)
+    np.savez_compressed(os.path.join(HERE, "retarded_field.npz"), names=np.array(list(rec)),
+                        **flat, **{f"geo__{k}": v for k, v in geo.items()})
+
+
 def main():
     lw.build(with_reference=True)
     if not lw.reference_available():
         raise SystemExit("the reference tree is needed to generate the fixtures")
     w, w2, tr1, tr4, ne = undulator_runs()
+    retarded_fields(tr1)
     loop_run()
     screens(w, w2, tr1, tr4, ne)
     range_errors()

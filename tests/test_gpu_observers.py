@@ -46,7 +46,8 @@ def test_cpp_observers_match_oracle(tmp_path):
     n = w.n_pix * w.nots * 6
     screen = data[:n].reshape(w.n_pix, w.nots, 6)
     mesh = data[n:2 * n].reshape(w.n_pix, w.nots, 6)
-    point = data[2 * n:].reshape(w.nots, 6)
+    point = data[2 * n:2 * n + w.nots * 6].reshape(w.nots, 6)
+    snap = data[2 * n + w.nots * 6:].reshape(s.nx * s.ny, 6)
     ref, rc = lw.integrate_screen(tr, w.pix_pos, w.pix_t0, w.dt, w.nots)
     assert rc == 0
     nrm = np.linalg.norm(ref)
@@ -54,3 +55,10 @@ def test_cpp_observers_match_oracle(tmp_path):
     assert np.array_equal(screen, mesh)
     c = (s.nx // 2) * s.ny + s.ny // 2
     assert np.linalg.norm(point - ref[c]) / np.linalg.norm(ref[c]) < 1e-5
+    # SnapshotObserver: cell (ix, iy) at O + dX (ix - (Nx-1)/2) + dY (iy - (Ny-1)/2)
+    ix, iy = np.meshgrid(np.arange(s.nx), np.arange(s.ny), indexing="ij")
+    cells = (np.asarray(s.origin)[None, :] + np.asarray(s.dx)[None, :] * (ix.reshape(-1, 1) - 0.5 * (s.nx - 1))
+             + np.asarray(s.dy)[None, :] * (iy.reshape(-1, 1) - 0.5 * (s.ny - 1)))
+    sref, rc = lw.retarded_field_at(tr, s.t0 + 0.5 * s.nots * s.dt, cells)
+    assert rc == 0 and np.abs(sref).max() > 0
+    np.testing.assert_allclose(snap, sref, rtol=1e-12, atol=1e-12 * np.abs(sref).max())

@@ -34,7 +34,7 @@ EXPORTED = [
     "teufel_cuda_point_decisions", "teufel_cuda_deposit_injected", "teufel_cuda_last_inwindow",
     "teufel_cuda_probe_peaks", "teufel_cuda_last_timing", "teufel_cuda_integrate_screen_noalloc",
     "teufel_cuda_batch_create", "teufel_cuda_batch_run", "teufel_cuda_batch_status",
-    "teufel_cuda_batch_free", "teufel_cuda_autotune",
+    "teufel_cuda_batch_free", "teufel_cuda_autotune", "teufel_cuda_retarded_field",
 ]
 
 # bytes of the fixed device array used by teufel_cuda_integrate_screen_noalloc
@@ -124,6 +124,9 @@ def lib():
         L.teufel_cuda_batch_run.argtypes = [_vp, _vp]
         L.teufel_cuda_batch_status.restype = ctypes.c_int
         L.teufel_cuda_batch_status.argtypes = [_vp, _lp, _lp, _dp]
+        L.teufel_cuda_retarded_field.restype = ctypes.c_int
+        L.teufel_cuda_retarded_field.argtypes = [_vp, ctypes.c_double, ctypes.c_int, _dp, _dp,
+                                                 _vp]
         L.teufel_cuda_autotune.restype = ctypes.c_int
         L.teufel_cuda_autotune.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int,
                                            ctypes.c_int, ctypes.POINTER(Options),
@@ -270,6 +273,15 @@ class TrajSet:
                                             ctypes.byref(nl), ctypes.byref(k), ctypes.byref(r)),
               "teufel_cuda_last_timing")
         return int(dep.value), int(nev.value), int(nl.value), float(k.value), float(r.value)
+
+    def retarded_field(self, obs_time, pos):
+        """teufel_cuda_retarded_field: the summed field [n, 6] at obs_time on
+        the points pos[n, 3] (the SnapshotObserver computation)."""
+        pos = _c(pos).reshape(-1, 3)
+        out = np.empty((pos.shape[0], 6))
+        check(lib().teufel_cuda_retarded_field(self.handle, obs_time, pos.shape[0], _ptr(pos),
+                                               _ptr(out), None), "teufel_cuda_retarded_field")
+        return out
 
     def autotune(self, pix_pos, pix_t0, dt, nots, n_pix=None, device=False):
         """teufel_cuda_autotune: (kernel_variant, n_slots, ms) of the fastest

@@ -124,6 +124,12 @@ cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const dou
                                       cudaStream_t s);
 int probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops);
 
+// RetardedField(t, X) summed over a particle set (lw_snapshot.cu): the
+// particle chunks to split a set into for np points, and the launch.
+int retarded_field_chunks(int np, int n_particles);
+cudaError_t launch_retarded_field(const DevTraj& tr, double obs_time, int np, const double* pos,
+                                  int n_chunks, double* partial, double* out, cudaStream_t s);
+
 // One work item of a batched launch: a pixel tile of an observer against one
 // slot (particle range) of its trajectory set.
 struct BatchItem {

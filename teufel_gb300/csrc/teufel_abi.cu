@@ -570,6 +570,37 @@ int teufel_cuda_autotune(const teufel_traj_set* traj_c, const double* pix_pos,
     return cleanup(TEUFEL_OK);
 }
 
+int teufel_cuda_retarded_field(const teufel_traj_set* traj_c, double obs_time, int Np,
+                               const double* pos, double* out, teufel_stream_t stream) {
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj_c);
+    if (!h || Np < 0 || (Np > 0 && (!pos || !out)) || !std::isfinite(obs_time))
+        return TEUFEL_ERR_ARG;
+    if (Np == 0) return TEUFEL_OK;
+    // a particle without trajectory points: the reference throws
+    // RANGEexception (src/particle.cpp:615)
+    for (int m = 0; m < h->dev.n_particles; m++)
+        if (h->h_seg_offsets[m + 1] == h->h_seg_offsets[m]) return TEUFEL_ERR_RANGE;
+    if (!finite_array(pos, 3 * (int64_t)Np)) return TEUFEL_ERR_ARG;
+    if (h->dev.n_particles == 0) {
+        std::memset(out, 0, sizeof(double) * 6 * (size_t)Np);
+        return TEUFEL_OK;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int n_chunks = retarded_field_chunks(Np, h->dev.n_particles);
+    int rc;
+    if ((rc = grow((void**)&h->d_pix, &h->pix_cap, sizeof(double) * 4 * (size_t)Np, false)) ||
+        (rc = grow((void**)&h->d_out, &h->out_cap, sizeof(double) * 6 * (size_t)Np, false)) ||
+        (rc = grow(&h->scratch, &h->scratch_bytes, sizeof(double) * 6 * (size_t)Np * n_chunks,
+                   false)))
+        return rc;
+    TRY_CUDA(cudaMemcpyAsync(h->d_pix, pos, sizeof(double) * 3 * Np, cudaMemcpyHostToDevice, s));
+    TRY_CUDA(launch_retarded_field(h->dev, obs_time, Np, h->d_pix, n_chunks,
+                                   static_cast<double*>(h->scratch), h->d_out, s));
+    TRY_CUDA(cudaMemcpyAsync(out, h->d_out, sizeof(double) * 6 * Np, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaStreamSynchronize(s));
+    return TEUFEL_OK;
+}
+
 int teufel_cuda_integrate_screen(const teufel_traj_set* traj, const double* pix_pos,
                                  const double* pix_t0, double dt, int Nt, int Np, double* out,
                                  teufel_stream_t s) {
