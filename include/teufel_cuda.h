@@ -93,6 +93,45 @@ int teufel_cuda_traj_upload(int n_particles, const int *n_points, const double *
                             const double *t, const double *x, const double *bg, const double *a,
                             teufel_traj_set **out);
 
+/* The field a device-tracked particle set moves through: the reference's
+ * Lattice of a PlanarUndulator (src/undulator.cpp:107-125, one-period linear
+ * ramps at both ends) centred at origin, plus a HomogeneousField
+ * (src/fields.cpp:150-163); either may be absent. */
+typedef struct teufel_lattice {
+    int has_undulator;
+    double b_peak;     /* peak field [T] */
+    double lambda_u;   /* period [m] */
+    int n_periods;
+    double origin[3];  /* undulator centre [m] */
+    int has_homogeneous;
+    double E[3];       /* [V/m] */
+    double B[3];       /* [T] */
+} teufel_lattice;
+
+/* Track particles on the device and keep the trajectories resident, without
+ * host trajectory arrays: the reference's ChargedParticle::InitVay and
+ * n_steps calls of StepVay (src/particle.cpp:407-512) per particle, giving
+ * n_steps+1 points, the first being the initial condition with the
+ * acceleration InitVay computes.
+ *   init[n][7]     t, x, y, z, beta*gamma x, y, z  (initTrajectory's arguments)
+ *   charge_e[n]    charge in units of e (the reference's Charge)
+ *   mass[n]        mass in electron masses (the reference's Mass)
+ *   tstep > 0, n_steps >= 0
+ * The result is a set like one from teufel_cuda_traj_upload, with charge
+ * Charge*ElementaryCharge.  FP64 in the reference's operation order: the
+ * trajectories agree with the reference's to within the last-ulp differences of
+ * sin/cos/sinh/cosh.  A non-finite trajectory returns TEUFEL_ERR_ARG. */
+int teufel_cuda_traj_track(int n_particles, const double *init, const double *charge_e,
+                           const double *mass, const teufel_lattice *lattice, double tstep,
+                           int n_steps, teufel_traj_set **out);
+
+/* Copy a set's trajectories back to the host, in teufel_cuda_traj_upload's
+ * layout: t[Npts], x[Npts][3], bg[Npts][3], a[Npts][3] (the reference's
+ * ChargedParticle::TrajTime/TrajPoint/TrajMomentum/TrajAccel, src/particle.h).
+ * Any pointer may be NULL. */
+int teufel_cuda_traj_download(const teufel_traj_set *traj, double *t, double *x, double *bg,
+                              double *a);
+
 /* Release a trajectory set and its device memory.  NULL is accepted. */
 int teufel_cuda_traj_free(teufel_traj_set *traj);
 

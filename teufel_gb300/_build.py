@@ -34,7 +34,7 @@ HARNESS_LIB = LIBDIR / "libteufel_harness.so"
 
 CU_SOURCES = ["teufel_abi.cu", "teufel_batch.cu", "lw_fp64.cu", "lw_fp32_main.cu",
               "lw_fp32_warp.cu", "lw_fp32_pair.cu", "lw_support.cu", "lw_noalloc.cu",
-              "lw_snapshot.cu"]
+              "lw_snapshot.cu", "lw_track.cu"]
 CU_HEADERS = ["lw_common.cuh", "lw_internal.h", "lw_fp32_point.cuh"]
 
 

@@ -35,6 +35,7 @@ EXPORTED = [
     "teufel_cuda_probe_peaks", "teufel_cuda_last_timing", "teufel_cuda_integrate_screen_noalloc",
     "teufel_cuda_batch_create", "teufel_cuda_batch_run", "teufel_cuda_batch_status",
     "teufel_cuda_batch_free", "teufel_cuda_autotune", "teufel_cuda_retarded_field",
+    "teufel_cuda_traj_track", "teufel_cuda_traj_download",
 ]
 
 # bytes of the fixed device array used by teufel_cuda_integrate_screen_noalloc
@@ -52,6 +53,25 @@ class ObserverDesc(ctypes.Structure):
     _fields_ = [("traj", ctypes.c_void_p), ("pix_pos", ctypes.c_void_p),
                 ("pix_t0", ctypes.c_void_p), ("dt", ctypes.c_double), ("Nt", ctypes.c_int),
                 ("Np", ctypes.c_int), ("out", ctypes.c_void_p)]
+
+
+class Lattice(ctypes.Structure):
+    """teufel_lattice: a planar undulator and/or a homogeneous field."""
+    _fields_ = [("has_undulator", ctypes.c_int), ("b_peak", ctypes.c_double),
+                ("lambda_u", ctypes.c_double), ("n_periods", ctypes.c_int),
+                ("origin", ctypes.c_double * 3), ("has_homogeneous", ctypes.c_int),
+                ("E", ctypes.c_double * 3), ("B", ctypes.c_double * 3)]
+
+
+def lattice(b_peak=0.0, lambda_u=1.0, n_periods=0, origin=(0.0, 0.0, 0.0), E=None, B=None):
+    L = Lattice()
+    L.has_undulator = 1 if n_periods > 0 else 0
+    L.b_peak, L.lambda_u, L.n_periods = b_peak, lambda_u, n_periods
+    L.origin[:] = list(origin)
+    L.has_homogeneous = 1 if (E is not None or B is not None) else 0
+    L.E[:] = list(E or (0.0, 0.0, 0.0))
+    L.B[:] = list(B or (0.0, 0.0, 0.0))
+    return L
 
 
 class TeufelError(RuntimeError):
@@ -124,6 +144,12 @@ def lib():
         L.teufel_cuda_batch_run.argtypes = [_vp, _vp]
         L.teufel_cuda_batch_status.restype = ctypes.c_int
         L.teufel_cuda_batch_status.argtypes = [_vp, _lp, _lp, _dp]
+        L.teufel_cuda_traj_track.restype = ctypes.c_int
+        L.teufel_cuda_traj_track.argtypes = [ctypes.c_int, _dp, _dp, _dp,
+                                             ctypes.POINTER(Lattice), ctypes.c_double,
+                                             ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        L.teufel_cuda_traj_download.restype = ctypes.c_int
+        L.teufel_cuda_traj_download.argtypes = [_vp, _dp, _dp, _dp, _dp]
         L.teufel_cuda_retarded_field.restype = ctypes.c_int
         L.teufel_cuda_retarded_field.argtypes = [_vp, ctypes.c_double, ctypes.c_int, _dp, _dp,
                                                  _vp]
@@ -193,6 +219,34 @@ class TrajSet:
         tr.n_particles = len(n_points)
         tr.n_points, tr.charge, tr.t, tr.x, tr.p, tr.a = n_points, charge, t, x, p, a
         return cls(tr)
+
+    @classmethod
+    def track(cls, init, charge_e, mass, lat, tstep, n_steps):
+        """teufel_cuda_traj_track: particles tracked on the device by the Vay
+        pusher through `lat` (abi.lattice(...)); init[n][7] = t, x, y, z,
+        beta*gamma; charge in units of e, mass in electron masses (arrays or
+        scalars)."""
+        init = _c(init).reshape(-1, 7)
+        n = init.shape[0]
+        ch = _c(np.broadcast_to(np.asarray(charge_e, dtype=np.float64), (n,)))
+        ms = _c(np.broadcast_to(np.asarray(mass, dtype=np.float64), (n,)))
+        h = _vp()
+        check(lib().teufel_cuda_traj_track(n, _ptr(init), _ptr(ch), _ptr(ms), ctypes.byref(lat),
+                                           tstep, n_steps, ctypes.byref(h)),
+              "teufel_cuda_traj_track")
+        obj = cls.__new__(cls)
+        obj.handle = h
+        obj.n_particles = n
+        obj.n_points = np.full(n, n_steps + 1, dtype=np.int32)
+        return obj
+
+    def download(self):
+        """(t, x, bg, a) of the set's trajectories (teufel_cuda_traj_download)."""
+        N = int(np.sum(self.n_points))
+        t, x, p, a = np.empty(N), np.empty((N, 3)), np.empty((N, 3)), np.empty((N, 3))
+        check(lib().teufel_cuda_traj_download(self.handle, _ptr(t), _ptr(x), _ptr(p), _ptr(a)),
+              "teufel_cuda_traj_download")
+        return t, x, p, a
 
     def free(self):
         if self.handle:

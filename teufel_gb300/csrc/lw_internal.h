@@ -124,6 +124,21 @@ cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const dou
                                       cudaStream_t s);
 int probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops);
 
+// The lattice the device pusher tracks through (lw_track.cu): a planar
+// undulator centred at `origin` and a homogeneous field; kz = 2 pi / lambda_u.
+struct TrackLattice {
+    int has_undulator;
+    double b_peak, lambda_u, kz;
+    int n_periods;
+    double origin[3];
+    int has_homogeneous;
+    double e[3], b[3];
+};
+cudaError_t launch_vay_track(int n, const double* init, const double* charge_e,
+                             const double* mass, const TrackLattice& L, double tstep, int n_steps,
+                             double4_32a* tx, double4_32a* pp, double4_32a* aa,
+                             unsigned int* status, cudaStream_t s);
+
 // RetardedField(t, X) summed over a particle set (lw_snapshot.cu): the
 // particle chunks to split a set into for np points, and the launch.
 int retarded_field_chunks(int np, int n_particles);

@@ -287,32 +287,12 @@ const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** stat
 }
 }  // namespace teufel
 
-extern "C" {
-
-void teufel_cuda_default_options(teufel_options* opt) {
-    if (!opt) return;
-    opt->precision = TEUFEL_PREC_FP32_SPLIT;
-    opt->device_pointers = 0;
-    opt->n_slots = 0;
-    opt->kernel_variant = 0;
-    opt->timing = 0;
-}
-
-const char* teufel_cuda_status_string(int status) {
-    switch (status) {
-        case TEUFEL_OK: return "ok";
-        case TEUFEL_ERR_ARG: return "bad argument";
-        case TEUFEL_ERR_NOMEM: return "out of memory";
-        case TEUFEL_ERR_CUDA: return "CUDA error";
-        case TEUFEL_ERR_RANGE: return "FieldTrace::add - index out of range.";
-        case TEUFEL_ERR_NODEVICE: return "no sm_103 CUDA device";
-        default: return "unknown status";
-    }
-}
-
-int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* charge_C,
-                            const double* t, const double* x, const double* bg, const double* a,
-                            teufel_traj_set** out) {
+// Builds a trajectory set: allocates the store, lets `fill` write the FP64
+// points (tx, pp, aa) of N > 0 points on stream s (synchronized on return),
+// then derives the FP32 per-point data and the pair layout.
+template <class Fill>
+int build_set(int n_particles, const int* n_points, const double* charge_C, Fill fill,
+              teufel_traj_set** out) {
     if (!out) return TEUFEL_ERR_ARG;
     *out = nullptr;
     if (n_particles < 0 || (n_particles > 0 && (!n_points || !charge_C))) return TEUFEL_ERR_ARG;
@@ -326,7 +306,6 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
         segs[m + 1] = segs[m] + nseg;
     }
     const int64_t N = offs[n_particles];
-    if (N > 0 && (!t || !x || !bg || !a)) return TEUFEL_ERR_ARG;
     // pairs (2j, 2j+1): as long as the longer particle
     const int n_pairs = (n_particles + 1) / 2;
     std::vector<int64_t> poffs(n_pairs + 1, 0), psegs(n_pairs + 1, 0);
@@ -392,24 +371,10 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
         cudaMemset(h->d_status, 0, sizeof(unsigned int)))
         return fail(cuda_fail(cudaGetLastError()));
     if (N > 0) {
-        // raw arrays to the device, then packed there
-        double* raw = nullptr;
-        if (cudaMalloc(&raw, sizeof(double) * 10 * (size_t)N) != cudaSuccess)
-            return fail(cuda_fail(cudaErrorMemoryAllocation));
-        double *rt = raw, *rx = raw + N, *rb = raw + 4 * N, *ra = raw + 7 * N;
-        cudaError_t e = cudaMemcpyAsync(rt, t, sizeof(double) * N, cudaMemcpyHostToDevice, s);
-        if (!e) e = cudaMemcpyAsync(rx, x, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
-        if (!e) e = cudaMemcpyAsync(rb, bg, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
-        if (!e) e = cudaMemcpyAsync(ra, a, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
-        if (!e) {
-            pack_points_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(
-                N, rt, rx, rb, ra, p_tx, p_pp, p_aa, h->d_status);
-            e = cudaGetLastError();
-        }
+        cudaError_t e = fill(d, s, h->d_status);
         if (!e) e = launch_prep_points(d, s);
         if (!e) e = launch_prep_pairs(d, s);
         cudaError_t e2 = cudaStreamSynchronize(s);
-        cudaFree(raw);
         if (e || e2) return fail(cuda_fail(e ? e : e2));
     } else if (n_particles > 0) {
         if (launch_prep_points(d, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
@@ -421,6 +386,137 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
     if (mask) return fail(status_from_mask(mask));
     *out = h;
     return TEUFEL_OK;
+}
+
+extern "C" {
+
+void teufel_cuda_default_options(teufel_options* opt) {
+    if (!opt) return;
+    opt->precision = TEUFEL_PREC_FP32_SPLIT;
+    opt->device_pointers = 0;
+    opt->n_slots = 0;
+    opt->kernel_variant = 0;
+    opt->timing = 0;
+}
+
+const char* teufel_cuda_status_string(int status) {
+    switch (status) {
+        case TEUFEL_OK: return "ok";
+        case TEUFEL_ERR_ARG: return "bad argument";
+        case TEUFEL_ERR_NOMEM: return "out of memory";
+        case TEUFEL_ERR_CUDA: return "CUDA error";
+        case TEUFEL_ERR_RANGE: return "FieldTrace::add - index out of range.";
+        case TEUFEL_ERR_NODEVICE: return "no sm_103 CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int teufel_cuda_traj_track(int n_particles, const double* init, const double* charge_e,
+                           const double* mass, const teufel_lattice* lat, double tstep,
+                           int n_steps, teufel_traj_set** out) {
+    if (!out) return TEUFEL_ERR_ARG;
+    *out = nullptr;
+    if (n_particles < 0 || n_steps < 0 || !lat || !(tstep > 0.0) || !std::isfinite(tstep) ||
+        (n_particles > 0 && (!init || !charge_e || !mass)))
+        return TEUFEL_ERR_ARG;
+    if (!finite_array(init, 7 * (int64_t)n_particles) || !finite_array(charge_e, n_particles) ||
+        !finite_array(mass, n_particles))
+        return TEUFEL_ERR_ARG;
+    for (int m = 0; m < n_particles; m++)
+        if (!(mass[m] != 0.0)) return TEUFEL_ERR_ARG;
+    if (lat->has_undulator && !(lat->lambda_u > 0.0)) return TEUFEL_ERR_ARG;
+    TrackLattice L{};
+    L.has_undulator = lat->has_undulator != 0;
+    L.b_peak = lat->b_peak;
+    L.lambda_u = lat->lambda_u;
+    L.kz = L.has_undulator ? 2.0 * kPi / lat->lambda_u : 0.0;  // src/undulator.cpp:79
+    L.n_periods = lat->n_periods;
+    L.has_homogeneous = lat->has_homogeneous != 0;
+    for (int k = 0; k < 3; k++) {
+        L.origin[k] = lat->origin[k];
+        L.e[k] = lat->E[k];
+        L.b[k] = lat->B[k];
+    }
+    if (n_steps >= (1 << 30)) return TEUFEL_ERR_ARG;
+    std::vector<int> npts(n_particles, n_steps + 1);
+    std::vector<double> charge_C(n_particles);
+    for (int m = 0; m < n_particles; m++) charge_C[m] = charge_e[m] * kE;  // Charge*ElementaryCharge
+    auto fill = [&](DevTraj& d, cudaStream_t s, unsigned int* status) -> cudaError_t {
+        double* buf = nullptr;
+        const size_t n = (size_t)n_particles;
+        cudaError_t e = cudaMalloc(&buf, sizeof(double) * 9 * n);
+        if (e) return e;
+        e = cudaMemcpyAsync(buf, init, sizeof(double) * 7 * n, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(buf + 7 * n, charge_e, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(buf + 8 * n, mass, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+        if (!e)
+            e = launch_vay_track(n_particles, buf, buf + 7 * n, buf + 8 * n, L, tstep, n_steps,
+                                 const_cast<double4_32a*>(d.tx), const_cast<double4_32a*>(d.pp),
+                                 const_cast<double4_32a*>(d.aa), status, s);
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        cudaFree(buf);
+        return e ? e : e2;
+    };
+    return build_set(n_particles, npts.data(), charge_C.data(), fill, out);
+}
+
+int teufel_cuda_traj_download(const teufel_traj_set* traj, double* t, double* x, double* bg,
+                              double* a) {
+    if (!traj) return TEUFEL_ERR_ARG;
+    const int64_t N = traj->dev.n_points;
+    if (N == 0) return TEUFEL_OK;
+    std::vector<double4_32a> buf((size_t)N);
+    const double4_32a* src[3] = {traj->dev.tx, traj->dev.pp, traj->dev.aa};
+    double* dst[3] = {x, bg, a};
+    for (int k = 0; k < 3; k++) {
+        if (!(dst[k] || (k == 0 && t))) continue;
+        TRY_CUDA(cudaMemcpy(buf.data(), src[k], sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < N; i++) {
+            const double4_32a v = buf[i];
+            if (k == 0) {
+                if (t) t[i] = v.x;
+                if (x) {
+                    x[3 * i] = v.y;
+                    x[3 * i + 1] = v.z;
+                    x[3 * i + 2] = v.w;
+                }
+            } else {
+                dst[k][3 * i] = v.x;
+                dst[k][3 * i + 1] = v.y;
+                dst[k][3 * i + 2] = v.z;
+            }
+        }
+    }
+    return TEUFEL_OK;
+}
+
+int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* charge_C,
+                            const double* t, const double* x, const double* bg, const double* a,
+                            teufel_traj_set** out) {
+    int64_t N = 0;
+    for (int m = 0; m < n_particles && n_points; m++) N += std::max(n_points[m], 0);
+    if (N > 0 && (!t || !x || !bg || !a)) return TEUFEL_ERR_ARG;
+    // the raw arrays to the device, then packed there (with a finite check)
+    auto fill = [&](DevTraj& d, cudaStream_t s, unsigned int* status) -> cudaError_t {
+        double* raw = nullptr;
+        cudaError_t e = cudaMalloc(&raw, sizeof(double) * 10 * (size_t)N);
+        if (e) return e;
+        double *rt = raw, *rx = raw + N, *rb = raw + 4 * N, *ra = raw + 7 * N;
+        e = cudaMemcpyAsync(rt, t, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(rx, x, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(rb, bg, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMemcpyAsync(ra, a, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+        if (!e) {
+            pack_points_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(
+                N, rt, rx, rb, ra, const_cast<double4_32a*>(d.tx), const_cast<double4_32a*>(d.pp),
+                const_cast<double4_32a*>(d.aa), status);
+            e = cudaGetLastError();
+        }
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        cudaFree(raw);
+        return e ? e : e2;
+    };
+    return build_set(n_particles, n_points, charge_C, fill, out);
 }
 
 int teufel_cuda_traj_free(teufel_traj_set* traj) {

@@ -263,7 +263,7 @@ def config1(nthreads: int = 0) -> Workload:
     scr = Screen((0.0, 0.0, 10.0), (0.01, 0.0, 0.0), (0.0, 0.01, 0.0), 21, 21,
                  t_arr - 1.0e-12, 5.0e-15, 2048)
     return Workload("config1", traj, scr.pixel_positions(), scr.pixel_t0(), scr.dt, scr.nots,
-                    dict(screen=scr, n_steps=n_steps, tstep=tstep))
+                    dict(screen=scr, n_steps=n_steps, tstep=tstep, lattice=lat))
 
 
 def _bunch_config(name, *, n_particles, total_charge, sx, sy, sz, eps_n, gamma0, rel_spread,
