@@ -425,9 +425,11 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
         rate, sample, _ = cpu_rate(w0, 12.0, nthreads)
+        rate1, sample1, _ = cpu_rate(w0, 5.0, 1)
         cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": sample + "; the oracle's C restatement of the reference's "
-                         "integrateFieldTrace, OpenMP over pixels"}
+                         "integrateFieldTrace, OpenMP over pixels",
+               "value_1_thread": rate1, "sample_1_thread": sample1}
 
     if rank == 0:
         frac_in = inwin / (evals_step * K) if K else 0.0

@@ -575,13 +575,18 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 }
                 const bool fast_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= 1u;
                 const bool fast_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= 1u;
-                // steps that certainly lie outside the window: nothing to add
-                const bool out_a = (q2.fla == 0 && A.Ba + q2.ka < 0) ||
-                                   (!(q1.fla & kExact) && A.Ba + q1.ka >= nt);
-                const bool out_b = (q2.flb == 0 && A.Bb + q2.kb < 0) ||
-                                   (!(q1.flb & kExact) && A.Bb + q1.kb >= nt);
-                const bool ok = (!dep_a || fast_a || out_a) && (!dep_b || fast_b || out_b);
-                if (__all_sync(0xffffffffu, ok)) {
+                bool go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a) && (!dep_b || fast_b));
+                if (!go_fast) {
+                    // steps that certainly lie outside the window add nothing
+                    // and leave the fast path open
+                    const bool out_a = (q2.fla == 0 && A.Ba + q2.ka < 0) ||
+                                       (!(q1.fla & kExact) && A.Ba + q1.ka >= nt);
+                    const bool out_b = (q2.flb == 0 && A.Bb + q2.kb < 0) ||
+                                       (!(q1.flb & kExact) && A.Bb + q1.kb >= nt);
+                    go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a || out_a) &&
+                                                          (!dep_b || fast_b || out_b));
+                }
+                if (go_fast) {
                     const bool da = dep_a && fast_a, db = dep_b && fast_b;
                     if (da || db) deposit_fast2(q1, q2, A.Ba, A.Bb, da, db, sink);
                     inwin += (unsigned)da + (unsigned)db;
