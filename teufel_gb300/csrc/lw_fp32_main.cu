@@ -70,6 +70,17 @@ __global__ void prep_particles_kernel(DevTraj tr, double4_32a* vhat) {
     vhat[m] = v;
 }
 
+// v <- R v in the set's frame (FP64)
+__device__ __forceinline__ void to_frame(const Frame& F, double& x, double& y, double& z) {
+    if (F.identity) return;
+    const double a = fma(F.r[0], x, fma(F.r[1], y, F.r[2] * z));
+    const double b = fma(F.r[3], x, fma(F.r[4], y, F.r[5] * z));
+    const double c = fma(F.r[6], x, fma(F.r[7], y, F.r[8] * z));
+    x = a;
+    y = b;
+    z = c;
+}
+
 __global__ void prep_points_kernel(DevTraj tr, float4* q0, float4* q1, float4* q2, float4* q3) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= tr.n_points) return;
@@ -97,7 +108,10 @@ __global__ void prep_points_kernel(DevTraj tr, float4* q0, float4* q1, float4* q
         double cd = kC * ddt;
         ceps = cd != 0.0 ? (cd - L) / cd : 1.0;  // 1 - |chord velocity|/c
     }
-    q0[i] = make_float4((float)(p.y - a.y), (float)(p.z - a.z), (float)(p.w - a.w), (float)ddt);
+    double ex = p.y - a.y, ey = p.z - a.z, ez = p.w - a.w;
+    to_frame(tr.frame, ex, ey, ez);
+    to_frame(tr.frame, cx, cy, cz);
+    q0[i] = make_float4((float)ex, (float)ey, (float)ez, (float)ddt);
     q3[i] = make_float4((float)cx, (float)cy, (float)cz, (float)ceps);
     double4_32a bg = tr.pp[i], ac = tr.aa[i];
     double P = sqrt(bg.x * bg.x + bg.y * bg.y + bg.z * bg.z);
@@ -109,18 +123,26 @@ __global__ void prep_points_kernel(DevTraj tr, float4* q0, float4* q1, float4* q
         bz = bg.z / P;
         eps = 1.0 / (gamma * (gamma + P));  // 1 - |beta| without cancellation
     }
+    to_frame(tr.frame, bx, by, bz);
     q1[i] = make_float4((float)bx, (float)by, (float)bz, (float)eps);
     double scale = field_scale(tr.charge[m]);
     double sa = scale / (gamma * kC);
-    q2[i] = make_float4((float)(ac.x * sa), (float)(ac.y * sa), (float)(ac.z * sa),
+    double ax = ac.x, ay = ac.y, az = ac.z;
+    to_frame(tr.frame, ax, ay, az);
+    q2[i] = make_float4((float)(ax * sa), (float)(ay * sa), (float)(az * sa),
                         (float)(scale / (gamma * gamma)));
 }
 
-cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s) {
+cudaError_t launch_prep_particles(const DevTraj& tr, cudaStream_t s) {
     if (tr.n_particles > 0) {
         prep_particles_kernel<<<(tr.n_particles + 127) / 128, 128, 0, s>>>(
             tr, const_cast<double4_32a*>(tr.vhat));
     }
+    return cudaGetLastError();
+}
+
+// After the set's frame is known (from the particles' directions).
+cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s) {
     if (tr.n_points > 0) {
         unsigned blocks = (unsigned)((tr.n_points + 255) / 256);
         prep_points_kernel<<<blocks, 256, 0, s>>>(tr, const_cast<float4*>(tr.q0),
@@ -179,7 +201,7 @@ __global__ void __launch_bounds__(128, 4)
         const double4_32a* txp = tr.tx + po;
         const float4 *q0 = tr.q0 + po, *q1 = tr.q1 + po, *q2 = tr.q2 + po, *q3 = tr.q3 + po;
         Anchor A;
-        make_anchor(A, txp[start], px);
+        make_anchor(A, txp[start], px, tr.frame);
         PointState p1, p2;
         point_field(p1, __ldg(q0 + start), __ldg(q1 + start), __ldg(q2 + start), A);
         start_chain(p1, A);
@@ -196,7 +218,7 @@ __global__ void __launch_bounds__(128, 4)
             if (boundary) {
                 const int i2c = i2 < npm ? i2 : ((npm - 1) & ~(kChunkLen - 1));
                 Anchor An;
-                make_anchor(An, txp[i2c], txp[i2c & ~(kSegLen - 1)], px);
+                make_anchor(An, txp[i2c], txp[i2c & ~(kSegLen - 1)], px, tr.frame);
                 rebase(p1, A, An);
                 A = An;
             }
@@ -305,7 +327,7 @@ __global__ void point_decisions_kernel(DevTraj tr, int m, double3 P, double t0, 
     const PixelCtx px = make_pixel(P, t0, dt, nt);
     const double4_32a* txp = tr.tx + o;
     Anchor A;
-    make_anchor(A, txp[start], px);
+    make_anchor(A, txp[start], px, tr.frame);
     PointState p1, p2;
     float comp = 0.0f, chain_err = 0.0f;
     for (int i = start; i < n && i < start + kSegLen; i++) {

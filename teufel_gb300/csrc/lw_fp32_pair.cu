@@ -515,8 +515,8 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 // borrows its partner's anchor (it never deposits)
                 const int wa = W.npa, wbn = W.npb;
                 const int ia = min(p0, wa - 1), ib = min(p0, wbn - 1);
-                if (wa > 0) make_anchor(aa, W.txa[ia], W.txa[ia & ~(kSegLen - 1)], px);
-                if (wbn > 0) make_anchor(ab, W.txb[ib], W.txb[ib & ~(kSegLen - 1)], px);
+                if (wa > 0) make_anchor(aa, W.txa[ia], W.txa[ia & ~(kSegLen - 1)], px, tr.frame);
+                if (wbn > 0) make_anchor(ab, W.txb[ib], W.txb[ib & ~(kSegLen - 1)], px, tr.frame);
                 else ab = aa;
                 if (wa <= 0) aa = ab;
                 const Anchor2 An = pack_anchor(aa, ab);

@@ -131,10 +131,18 @@ struct Anchor {
 // from point b (the first point of a's segment, to which the per-point
 // offsets e are relative).
 __device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const double4_32a b,
-                                            const PixelCtx& px) {
-    A.Dx = (float)(px.P.x - b.y);
-    A.Dy = (float)(px.P.y - b.z);
-    A.Dz = (float)(px.P.z - b.w);
+                                            const PixelCtx& px, const Frame& F) {
+    const double dx = px.P.x - b.y, dy = px.P.y - b.z, dz = px.P.z - b.w;
+    if (F.identity) {
+        A.Dx = (float)dx;
+        A.Dy = (float)dy;
+        A.Dz = (float)dz;
+    } else {
+        // the distance vector in the set's frame, formed in FP64
+        A.Dx = (float)fma(F.r[0], dx, fma(F.r[1], dy, F.r[2] * dz));
+        A.Dy = (float)fma(F.r[3], dx, fma(F.r[4], dy, F.r[5] * dz));
+        A.Dz = (float)fma(F.r[6], dx, fma(F.r[7], dy, F.r[8] * dz));
+    }
     const double pa = fma(px.Ph.x, a.y, fma(px.Ph.y, a.z, px.Ph.z * a.w));  // P^.x
     const double L = px.Pn - pa;
     const double cx = a.z * px.Ph.z - a.w * px.Ph.y;
@@ -167,8 +175,9 @@ __device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, cons
     A.err = own + px.refb0 + (float)(fabs(a.x) * px.inv_dt * 4.5e-16);
     if (u != u0) A.err = 1.0f;  // clamped: resolve the segment exactly
 }
-__device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const PixelCtx& px) {
-    make_anchor(A, a, a, px);
+__device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const PixelCtx& px,
+                                            const Frame& F) {
+    make_anchor(A, a, a, px, F);
 }
 
 struct PointState {

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kWThreads, MINB)
                                 warp_any_above(chain_err, kReanchorBound);
             if (anchor) {
                 Anchor An;
-                make_anchor(An, txp[p0], txp[p0 & ~(kSegLen - 1)], px);
+                make_anchor(An, txp[p0], txp[p0 & ~(kSegLen - 1)], px, tr.frame);
                 if (c > 0) rebase(p1, A, An);
                 A = An;
             }

@@ -24,6 +24,16 @@ constexpr int kSegLen = 1 << kSegShift;
 constexpr int kChunkShift = 5;
 constexpr int kChunkLen = 1 << kChunkShift;
 
+// The frame the FP32 per-point vectors of a set are expressed in: v' = R v
+// (row-major r).  Its z axis is the set's mean direction of motion, so that
+// the transverse components of all directions that matter stay small and
+// FP32 keeps their angles to ~1e-7 relative; identity = 1 when the set moves
+// along a coordinate axis already (then nothing is rotated).
+struct Frame {
+    double r[9];
+    int identity;
+};
+
 // Device view of a resident trajectory set.
 struct DevTraj {
     int n_particles;
@@ -51,6 +61,7 @@ struct DevTraj {
     //   (chx a, chx b, chy a, chy b) (chz a, chz b, ceps a, ceps b)
     // where b = beta-hat, c = q2, ch = chord direction; beyond the end of the
     // shorter particle its last point is repeated.
+    Frame frame;
     int n_pairs;
     int64_t n_pair_segments;
     const int64_t* pair_offsets;      // [n_pairs+1] first pair-point of each pair
@@ -75,6 +86,7 @@ struct DevWork {
     void* scratch;            // per-slot partial traces
     int64_t slot_stride;      // elements between slots
     unsigned int* status;     // bit mask of TEUFEL_ERR_* seen on the device
+    Frame frame;              // the set's frame: the FP32 reduction turns fields back
     unsigned long long* counters;  // [0] in-window triples, [1] exact-fallback points,
                                    // [2] bin contributions (deposits), [3] point
                                    // evaluations (in window or walked for a neighbour)
@@ -114,6 +126,7 @@ cudaError_t launch_point_decisions(const DevTraj& tr, int m, double3 pos, double
 cudaError_t launch_deposit_injected(int n_part, const int64_t* offs, const double* ts,
                                     const double* f, double t0, double dt, int nt, int precision,
                                     double* trace, unsigned int* status, cudaStream_t s);
+cudaError_t launch_prep_particles(const DevTraj& tr, cudaStream_t s);
 cudaError_t launch_prep_points(const DevTraj& tr, cudaStream_t s);
 cudaError_t launch_prep_pairs(const DevTraj& tr, cudaStream_t s);
 cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,

@@ -131,6 +131,7 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
         w.scratch = sym->scratch;
         w.slot_stride = (int64_t)Np * Nt * 6;
         w.status = d_status;
+        w.frame = tr->frame;
         w.counters = nullptr;
         e = launch_fp32(*tr, sc, w, kVariantUniform, s);
         if (!e) e = launch_reduce_fp32(w, sc, d_out, s);

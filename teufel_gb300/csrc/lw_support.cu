@@ -34,6 +34,17 @@ __device__ __forceinline__ void reduce_fp32_bin(const DevWork& w, int64_t e, dou
             __stcs(p + 1, z);
             __stcs(p + 2, z);
         }
+        if (!w.frame.identity) {
+            // from the set's frame back to the observer's: v = R^T v'
+            const double* r = w.frame.r;
+#pragma unroll
+            for (int k = 0; k < 6; k += 3) {
+                const double a = acc[k], b = acc[k + 1], c = acc[k + 2];
+                acc[k] = fma(r[0], a, fma(r[3], b, r[6] * c));
+                acc[k + 1] = fma(r[1], a, fma(r[4], b, r[7] * c));
+                acc[k + 2] = fma(r[2], a, fma(r[5], b, r[8] * c));
+            }
+        }
         double* o = out + e * 6;
         o[0] += acc[0];
         o[1] += acc[1];

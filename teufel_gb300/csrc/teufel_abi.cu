@@ -44,6 +44,7 @@ struct teufel_traj_set {
     bool last_timed = false;
     std::vector<int64_t> h_seg_offsets;
     int last_slots = 0;
+    bool counted = false;  // included in the live-set count of its device
 };
 
 namespace {
@@ -136,6 +137,47 @@ bool finite_array(const double* p, int64_t n) {
 
 // Device part of an integration: partial traces per slot, then the FP64
 // reduction into out (device pointers).  Enqueued on s.
+// ---- partial-trace memory ----
+// The FP32 partial traces of an integration come from a stream-ordered pool
+// of the library's own, one per device, allocated on the call's stream and
+// returned to the pool when the call's work is done.  Trajectory handles thus
+// share this memory instead of each keeping its own; the pool keeps what it
+// has (no release threshold) until the last handle of the device is freed.
+std::mutex g_pool_mu;
+std::map<int, cudaMemPool_t> g_pools;
+std::map<int, int> g_live_sets;
+
+cudaMemPool_t scratch_pool(int dev) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pools.find(dev);
+    if (it != g_pools.end()) return it->second;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pools[dev] = pool;
+    return pool;
+}
+
+// Free device memory plus what the pool holds but does not use.
+size_t available_bytes(cudaMemPool_t pool) {
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    uint64_t reserved = 0, used = 0;
+    if (pool) {
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    }
+    return free_b + (size_t)(reserved > used ? reserved - used : 0);
+}
+
 // ---- tuned choices per shape class (teufel_cuda_autotune) ----
 struct TuneKey {
     int np, nt, parts, pts;  // log2 buckets of pixels, samples, particles, points/particle
@@ -203,13 +245,22 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         slots_total = std::max<int64_t>(slots_total,
                                         (units + max_units_per_slot - 1) / max_units_per_slot);
     slots_total = std::min<int64_t>(slots_total, std::max<int64_t>(G, 1));
-    size_t free_b = 0, total_b = 0;
-    cudaMemGetInfo(&free_b, &total_b);
-    size_t budget = std::min<size_t>((size_t)48 << 30, (size_t)(0.4 * (double)(free_b + h->scratch_bytes)));
+    cudaMemPool_t pool = scratch_pool(h->device);
+    if (!pool) return TEUFEL_ERR_CUDA;
+    size_t budget = std::min<size_t>((size_t)48 << 30,
+                                     (size_t)(0.4 * (double)available_bytes(pool)));
     int64_t per_pass = slot_bytes ? (int64_t)(budget / slot_bytes) : slots_total;
     per_pass = std::max<int64_t>(1, std::min<int64_t>(per_pass, slots_total));
-    int rc = grow(&h->scratch, &h->scratch_bytes, slot_bytes * (size_t)per_pass, true);
-    if (rc) return rc;
+    const size_t scratch_bytes = std::max<size_t>(slot_bytes * (size_t)per_pass, 256);
+    void* scratch = nullptr;
+    TRY_CUDA(cudaMallocFromPoolAsync(&scratch, scratch_bytes, pool, s));
+    // returned to the pool on every exit, in stream order after the work
+    struct Release {
+        void* p;
+        cudaStream_t s;
+        ~Release() { cudaFreeAsync(p, s); }
+    } release{scratch, s};
+    TRY_CUDA(cudaMemsetAsync(scratch, 0, scratch_bytes, s));
     h->last_slots = (int)slots_total;
     std::vector<int64_t> bounds(slots_total + 1);
     for (int64_t k = 0; k <= slots_total; k++) bounds[k] = G * k / slots_total;
@@ -240,9 +291,10 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         DevWork w;
         w.n_slots = (int)std::min<int64_t>(per_pass, slots_total - p0);
         w.slot_seg = h->slot_seg + p0;
-        w.scratch = h->scratch;
+        w.scratch = scratch;
         w.slot_stride = (int64_t)np * nt * 6;
         w.status = h->d_status;
+        w.frame = h->dev.frame;
         w.counters = h->d_counters;
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used], s));
         cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
@@ -286,6 +338,56 @@ const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** stat
     return &traj->dev;
 }
 }  // namespace teufel
+
+Frame identity_frame() {
+    Frame f{};
+    f.r[0] = f.r[4] = f.r[8] = 1.0;
+    f.identity = 1;
+    return f;
+}
+
+// The set's frame from its particles' directions of motion (vhat, the first
+// to last point of each trajectory): z' along their mean.  A set moving
+// within 1e-4 rad of a coordinate axis keeps the identity, which leaves its
+// arithmetic untouched.
+cudaError_t set_frame(DevTraj& d) {
+    d.frame = identity_frame();
+    if (d.n_particles == 0) return cudaSuccess;
+    std::vector<double4_32a> v((size_t)d.n_particles);
+    cudaError_t e = cudaMemcpy(v.data(), d.vhat, sizeof(double4_32a) * v.size(),
+                               cudaMemcpyDeviceToHost);
+    if (e) return e;
+    double n[3] = {0.0, 0.0, 0.0};
+    for (const auto& q : v) {
+        n[0] += q.x;
+        n[1] += q.y;
+        n[2] += q.z;
+    }
+    const double L = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(L > 0.0)) return cudaSuccess;
+    for (double& c : n) c /= L;
+    const double big = std::max(std::fabs(n[0]), std::max(std::fabs(n[1]), std::fabs(n[2])));
+    if (big > 1.0 - 5.0e-9) return cudaSuccess;  // along an axis already
+    // x' from the coordinate axis least aligned with n, made orthogonal to n
+    int k = 0;
+    for (int j = 1; j < 3; j++)
+        if (std::fabs(n[j]) < std::fabs(n[k])) k = j;
+    double ax[3] = {0.0, 0.0, 0.0};
+    ax[k] = 1.0;
+    const double an = ax[0] * n[0] + ax[1] * n[1] + ax[2] * n[2];
+    double ex[3] = {ax[0] - an * n[0], ax[1] - an * n[1], ax[2] - an * n[2]};
+    const double le = std::sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
+    for (double& c : ex) c /= le;
+    const double ey[3] = {n[1] * ex[2] - n[2] * ex[1], n[2] * ex[0] - n[0] * ex[2],
+                          n[0] * ex[1] - n[1] * ex[0]};
+    for (int j = 0; j < 3; j++) {
+        d.frame.r[j] = ex[j];
+        d.frame.r[3 + j] = ey[j];
+        d.frame.r[6 + j] = n[j];
+    }
+    d.frame.identity = 0;
+    return cudaSuccess;
+}
 
 // Builds a trajectory set: allocates the store, lets `fill` write the FP64
 // points (tx, pp, aa) of N > 0 points on stream s (synchronized on return),
@@ -370,20 +472,29 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
          cudaMemcpy(p_charge, charge_C, sizeof(double) * n_particles, cudaMemcpyHostToDevice)) ||
         cudaMemset(h->d_status, 0, sizeof(unsigned int)))
         return fail(cuda_fail(cudaGetLastError()));
+    d.frame = identity_frame();
     if (N > 0) {
         cudaError_t e = fill(d, s, h->d_status);
+        if (!e) e = launch_prep_particles(d, s);
+        if (!e) e = cudaStreamSynchronize(s);
+        if (!e) e = set_frame(d);
         if (!e) e = launch_prep_points(d, s);
         if (!e) e = launch_prep_pairs(d, s);
         cudaError_t e2 = cudaStreamSynchronize(s);
         if (e || e2) return fail(cuda_fail(e ? e : e2));
     } else if (n_particles > 0) {
-        if (launch_prep_points(d, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        if (launch_prep_particles(d, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
             return fail(cuda_fail(cudaGetLastError()));
     }
     unsigned int mask = 0;
     if (cudaMemcpy(&mask, h->d_status, sizeof(mask), cudaMemcpyDeviceToHost) != cudaSuccess)
         return fail(cuda_fail(cudaGetLastError()));
     if (mask) return fail(status_from_mask(mask));
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        g_live_sets[h->device]++;
+        h->counted = true;
+    }
     *out = h;
     return TEUFEL_OK;
 }
@@ -521,6 +632,17 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
 
 int teufel_cuda_traj_free(teufel_traj_set* traj) {
     if (!traj) return TEUFEL_OK;
+    if (traj->counted) {
+        // the last set of a device gives the partial-trace pool's memory back
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        if (--g_live_sets[traj->device] == 0) {
+            auto it = g_pools.find(traj->device);
+            if (it != g_pools.end()) {
+                cudaDeviceSynchronize();
+                cudaMemPoolTrimTo(it->second, 0);
+            }
+        }
+    }
     for (void* p : traj->owned) cudaFree(p);
     if (traj->scratch) cudaFree(traj->scratch);
     if (traj->slot_seg) cudaFree(traj->slot_seg);

@@ -182,6 +182,7 @@ int teufel_cuda_batch_create(int n_obs, const teufel_observer* obs, const teufel
         w.slot_seg = d_seg + h_seg.size();
         for (int64_t s = 0; s <= p.slots; s++) h_seg.push_back(t.n_pair_segments * s / p.slots);
         w.scratch = d_scratch + scratch_off;
+        w.frame = t.frame;
         w.slot_stride = (int64_t)ob.Np * ob.Nt * 6;
         w.status = b->d_status;
         w.counters = b->d_counters;
