@@ -19,6 +19,7 @@ TEUFEL_ERR_ARG = 1
 TEUFEL_ERR_NOMEM = 2
 TEUFEL_ERR_CUDA = 3
 TEUFEL_ERR_RANGE = 4
+TEUFEL_ERR_TIMEOUT = 5
 TEUFEL_ERR_NODEVICE = 6
 
 E_CHARGE = 1.6021766208e-19  # src/global.h:36

@@ -221,6 +221,14 @@ __device__ __forceinline__ PointState unpack(const PointState2& S) {
     return p;
 }
 
+// red.global.add.v2.f32 under a predicate: the L2 adds the pair when p holds.
+__device__ __forceinline__ void red_add2_if(bool p, float* addr, float a, float b) {
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %0, 0;\n\t@q red.global.add.v2.f32 [%1], {%2, %3};\n\t}"
+        ::"r"((int)p), "l"(addr), "f"(a), "f"(b)
+        : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // The sink of a lane: one pixel row, an open bin per particle, accumulators
 // in packed form (component c of particles a and b).  Closed bins are added
@@ -293,32 +301,42 @@ struct PairSink {
     // crosses into bin k+1.
     __device__ __forceinline__ void add_fast(bool fa, bool fb, int ka, int kb, bool sa, bool sb,
                                              const F2* f1, const F2* f2v) {
-        if (fa && ka != open_a) {
-            flush<0>();
-            open_a = ka;
+        // a bin other than the open one: only after a general-path step or at
+        // the start of a walk, so one branch for both particles
+        const bool na = fa && ka != open_a, nb = fb && kb != open_b;
+        if (na || nb) {
+            if (na) {
+                flush<0>();
+                open_a = ka;
 #pragma unroll
-            for (int c = 0; c < 6; c++) acc[c].v.x = 0.0f;
-        }
-        if (fb && kb != open_b) {
-            flush<1>();
-            open_b = kb;
+                for (int c = 0; c < 6; c++) acc[c].v.x = 0.0f;
+            }
+            if (nb) {
+                flush<1>();
+                open_b = kb;
 #pragma unroll
-            for (int c = 0; c < 6; c++) acc[c].v.y = 0.0f;
+                for (int c = 0; c < 6; c++) acc[c].v.y = 0.0f;
+            }
         }
 #pragma unroll
         for (int c = 0; c < 6; c++) acc[c] = acc[c] + f1[c];
-        if (sa) {
-            reduce_to<0>(ka);
-            open_a = ka + 1;
-        }
-        if (sb) {
-            reduce_to<1>(kb);
-            open_b = kb + 1;
-        }
+        // a step that crosses into the next bin closes its bin: predicated
+        // reductions, no divergent branch
+        reduce_if<0>(sa, ka);
+        reduce_if<1>(sb, kb);
+        open_a = sa ? ka + 1 : open_a;
+        open_b = sb ? kb + 1 : open_b;
         const F2 keep = f2(sa ? 0.0f : 1.0f, sb ? 0.0f : 1.0f);
 #pragma unroll
         for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, f2v[c]);
         n_add += (unsigned)fa + (unsigned)fb + (unsigned)sa + (unsigned)sb;
+    }
+    template <int W>
+    __device__ __forceinline__ void reduce_if(bool p, int k) {
+        float* q = row + (int64_t)k * 6;
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            red_add2_if(p, q + 2 * c, get<W>(2 * c), get<W>(2 * c + 1));
     }
 };
 
@@ -549,29 +567,29 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 const bool dep_a = i > start && i <= lim_a;
                 const bool dep_b = i > start && i <= lim_b;
                 const int nt = sc.nt;
-                if (0.5f - fabsf(q2.r.v.x) <= chain_err.v.x && i <= lim_a) {
-                    const ExactPoint e = exact_point(W.txa, i, px, A.Ba);
-                    q2.ka = e.ki;
-                    q2.r.v.x = e.r;
-                    q2.idxa = e.idx;
-                    q2.fla = e.flags;
-                    atomicAdd(&sh.stats[1], 1ull);
-                    q2.rega = false;
-                } else {
-                    q2.fla = 0;
-                    q2.rega = (unsigned)(A.Ba + q2.ka) < (unsigned)nt;
-                }
-                if (0.5f - fabsf(q2.r.v.y) <= chain_err.v.y && i <= lim_b) {
-                    const ExactPoint e = exact_point(W.txb, i, px, A.Bb);
-                    q2.kb = e.ki;
-                    q2.r.v.y = e.r;
-                    q2.idxb = e.idx;
-                    q2.flb = e.flags;
-                    atomicAdd(&sh.stats[1], 1ull);
-                    q2.regb = false;
-                } else {
-                    q2.flb = 0;
-                    q2.regb = (unsigned)(A.Bb + q2.kb) < (unsigned)nt;
+                const bool near_a = 0.5f - fabsf(q2.r.v.x) <= chain_err.v.x && i <= lim_a;
+                const bool near_b = 0.5f - fabsf(q2.r.v.y) <= chain_err.v.y && i <= lim_b;
+                q2.fla = 0;
+                q2.flb = 0;
+                q2.rega = !near_a && (unsigned)(A.Ba + q2.ka) < (unsigned)nt;
+                q2.regb = !near_b && (unsigned)(A.Bb + q2.kb) < (unsigned)nt;
+                if (near_a || near_b) {  // rare: one branch for both particles
+                    if (near_a) {
+                        const ExactPoint e = exact_point(W.txa, i, px, A.Ba);
+                        q2.ka = e.ki;
+                        q2.r.v.x = e.r;
+                        q2.idxa = e.idx;
+                        q2.fla = e.flags;
+                        atomicAdd(&sh.stats[1], 1ull);
+                    }
+                    if (near_b) {
+                        const ExactPoint e = exact_point(W.txb, i, px, A.Bb);
+                        q2.kb = e.ki;
+                        q2.r.v.y = e.r;
+                        q2.idxb = e.idx;
+                        q2.flb = e.flags;
+                        atomicAdd(&sh.stats[1], 1ull);
+                    }
                 }
                 const bool fast_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= 1u;
                 const bool fast_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= 1u;
@@ -588,7 +606,9 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 }
                 if (go_fast) {
                     const bool da = dep_a && fast_a, db = dep_b && fast_b;
-                    if (da || db) deposit_fast2(q1, q2, A.Ba, A.Bb, da, db, sink);
+                    // unconditional: a particle without a deposit adds zeros (its
+                    // fields are finite for any observer off its trajectory)
+                    deposit_fast2(q1, q2, A.Ba, A.Bb, da, db, sink);
                     inwin += (unsigned)da + (unsigned)db;
                 } else {
                     if (dep_a) {

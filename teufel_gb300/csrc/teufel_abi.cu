@@ -517,6 +517,7 @@ const char* teufel_cuda_status_string(int status) {
         case TEUFEL_ERR_NOMEM: return "out of memory";
         case TEUFEL_ERR_CUDA: return "CUDA error";
         case TEUFEL_ERR_RANGE: return "FieldTrace::add - index out of range.";
+        case TEUFEL_ERR_TIMEOUT: return "device wait timed out";
         case TEUFEL_ERR_NODEVICE: return "no sm_103 CUDA device";
         default: return "unknown status";
     }
