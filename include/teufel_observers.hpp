@@ -3,8 +3,11 @@
 //
 // Mirrors, with the same member names, argument meaning and error behaviour:
 //   BaseObserver / Observer<SourceT>     src/observer.h:43-146
-//   ScreenObserver<Beam>                 src/screen.h, src/screen.cpp:34-146, 240-296
-//   MeshedScreen<Beam> (integrate/buffer) src/mesh.cpp:289-316, 376-425
+//   ScreenObserver<Beam>                 src/screen.h, src/screen.cpp:34-146, 240-560
+//   MeshedScreen<Beam> (read, init, integrate, buffer, writeFile, totalEnergy)
+//                                        src/mesh.cpp:31-278, 289-316, 376-754
+// HDF5 files are read and written by teufel_hdf5_read.hpp / teufel_hdf5_write.hpp
+// (no HDF5 library needed); the PointObserver trace is written as SDDS.
 //   PointObserver<Beam>                  src/point_observer.cpp:30-110
 //   FieldTrace (t0, dt, N, add, buffer)  src/fieldtrace.h, src/fieldtrace.cpp
 //   IOexception                          src/global.h:75-84
@@ -18,6 +21,8 @@
 // device for every observer that integrates from it.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +31,8 @@
 #include <vector>
 
 #include "teufel_cuda.h"
+#include "teufel_hdf5_read.hpp"
+#include "teufel_hdf5_write.hpp"
 
 namespace teufel_gb300 {
 
@@ -49,7 +56,30 @@ struct Vector {
     Vector(double a, double b, double c) : x(a), y(b), z(c) {}
     Vector operator+(const Vector& o) const { return Vector(x + o.x, y + o.y, z + o.z); }
     Vector operator*(double f) const { return Vector(x * f, y * f, z * f); }
+    Vector operator-(const Vector& o) const { return Vector(x - o.x, y - o.y, z - o.z); }
+    Vector& operator+=(const Vector& o) {
+        x += o.x;
+        y += o.y;
+        z += o.z;
+        return *this;
+    }
+    double norm() const { return std::sqrt(x * x + y * y + z * z); }
+    // divides by the norm unguarded, as src/vector.cpp:137-143 does
+    void normalize() {
+        const double n = norm();
+        x /= n;
+        y /= n;
+        z /= n;
+    }
 };
+
+inline double dot(const Vector& a, const Vector& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline Vector cross(const Vector& a, const Vector& b) {
+    return Vector(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// vacuum permeability [Vs/Am], as the reference defines it (src/global.h:43)
+constexpr double kMuNull = 4.0 * 3.1415926535897932384626433832795029 * 1e-7;
 
 // One electromagnetic sample: Ex, Ey, Ez, Bx, By, Bz (the ElMagField layout).
 struct ElMagField {
@@ -145,11 +175,19 @@ public:
 // Nx x Ny rectangular screen (src/screen.cpp:34-110).
 class ScreenObserver : public Observer<TrajectorySource> {
 public:
+    // filename is where generateOutput() writes the HDF5 file
+    ScreenObserver(std::string filename, Vector position, Vector dx, Vector dy, unsigned int nx,
+                   unsigned int ny, double t0, double dt, double dtx, double dty, unsigned int nots)
+        : FileName(std::move(filename)), Origin(position), dX(dx), dY(dy), Nx(nx), Ny(ny),
+          t0_obs(t0), dt_obs(dt), dtx_obs(dtx), dty_obs(dty), NOTS(nots),
+          buf((std::size_t)nx * ny * nots * 6, 0.0) {
+        normal = cross(dX, dY) * -1.0;  // the backward normal, src/screen.cpp:52-53
+        normal.normalize();
+    }
     ScreenObserver(Vector position, Vector dx, Vector dy, unsigned int nx, unsigned int ny,
                    double t0, double dt, double dtx, double dty, unsigned int nots)
-        : Origin(position), dX(dx), dY(dy), Nx(nx), Ny(ny), t0_obs(t0), dt_obs(dt),
-          dtx_obs(dtx), dty_obs(dty), NOTS(nots),
-          buf((std::size_t)nx * ny * nots * 6, 0.0) {}
+        : ScreenObserver(std::string(), position, dx, dy, nx, ny, t0, dt, dtx, dty, nots) {}
+    Vector getNormal() const { return normal; }
 
     // center index is Nx/2, Ny/2 with integer division (src/screen.cpp:97-103)
     Vector CellPosition(unsigned int ix, unsigned int iy) const {
@@ -196,35 +234,172 @@ public:
             throw IOexception("ScreenObserver::fromBuffer() - buffer size mismatch.");
         std::memcpy(buf.data(), buffer, sizeof(double) * size);
     }
-    // The reference writes HDF5 here (ScreenObserver::WriteTimeDomainFieldHDF5 (src/screen.cpp:298-560)); this build
-    // has no HDF5 library, so the traces leave through getBuffer().
-    void generateOutput() override {
-        throw IOexception("ScreenObserver::generateOutput - HDF5 output is not available in this build");
+    // The HDF5 layout of src/screen.cpp:298-560: ObservationPosition
+    // [Nx][Ny][3] (attributes Nx, Ny), Screen [4][3] = origin, normal, dX, dY
+    // (Nx, Ny, NOTS, t0, dt, dtx, dty) and ElMagField [Nx][Ny][NOTS][6]
+    // (t0, dt, NOTS).
+    void WriteTimeDomainFieldHDF5() {
+        if (FileName.empty())
+            throw IOexception("ScreenObserver::WriteTimeDomainFieldHDF5 - no file name given");
+        std::vector<double> pos((std::size_t)Nx * Ny * 3);
+        for (unsigned int ix = 0; ix < Nx; ix++)
+            for (unsigned int iy = 0; iy < Ny; iy++) {
+                const Vector c = CellPosition(ix, iy);
+                double* q = &pos[((std::size_t)ix * Ny + iy) * 3];
+                q[0] = c.x;
+                q[1] = c.y;
+                q[2] = c.z;
+            }
+        const double screen[12] = {Origin.x, Origin.y, Origin.z, normal.x, normal.y, normal.z,
+                                   dX.x,     dX.y,     dX.z,     dY.x,     dY.y,     dY.z};
+        using h5::AttrOut;
+        try {
+            h5::Writer w;
+            w.add("ObservationPosition", {Nx, Ny, 3}, pos.data(),
+                  {AttrOut::Int("Nx", (int32_t)Nx), AttrOut::Int("Ny", (int32_t)Ny)});
+            w.add("Screen", {4, 3}, screen,
+                  {AttrOut::Int("Nx", (int32_t)Nx), AttrOut::Int("Ny", (int32_t)Ny),
+                   AttrOut::Int("NOTS", (int32_t)NOTS), AttrOut::Double("t0", t0_obs),
+                   AttrOut::Double("dt", dt_obs), AttrOut::Double("dtx", dtx_obs),
+                   AttrOut::Double("dty", dty_obs)});
+            w.add("ElMagField", {Nx, Ny, NOTS, 6}, buf.data(),
+                  {AttrOut::Double("t0", t0_obs), AttrOut::Double("dt", dt_obs),
+                   AttrOut::Int("NOTS", (int32_t)NOTS)});
+            w.write(FileName);
+        } catch (const h5::Error& e) {
+            throw IOexception(std::string("ScreenObserver::WriteTimeDomainFieldHDF5 - ") + e.what());
+        }
     }
+    void generateOutput() override { WriteTimeDomainFieldHDF5(); }
     void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
 
 private:
-    Vector Origin, dX, dY;
+    std::string FileName;
+    Vector Origin, dX, dY, normal;
     unsigned int Nx, Ny;
     double t0_obs, dt_obs, dtx_obs, dty_obs;
     unsigned int NOTS;
     std::vector<double> buf;  // [Nx][Ny][NOTS][6]
 };
 
-// Observation points with individual trace start times (the integrate and
-// buffer part of MeshedScreen, src/mesh.cpp:289-316, 376-425).
+// A screen of triangular cells, each observed at one point with its own trace
+// start time (src/mesh.h, src/mesh.cpp).
 class MeshedScreen : public Observer<TrajectorySource> {
 public:
+    // Reads the mesh as MeshedScreen(std::string) does (src/mesh.cpp:31-218):
+    // MeshCornerPoints [Ncp][3] (attribute Ncp), ObservationPosition [Np][3]
+    // (attribute Np), MeshTriangles [Np][3] corner indices, and when present
+    // ObservationTime [Np] (attributes Nt, dt) and ElMagField [Np][Nt][6].
+    // Without ObservationTime the traces are empty (t0 = dt = 0, Nt = 0).
+    explicit MeshedScreen(const std::string& filename) : FileName(filename) {
+        try {
+            load(filename);
+        } catch (const h5::Error& e) {
+            throw IOexception(std::string("MeshedScreen - ") + e.what());
+        }
+    }
+    // A mesh given directly: observation points with their start times.
     MeshedScreen(std::vector<Vector> points, std::vector<double> t0, double dt, int nt)
         : pts(std::move(points)), T0(std::move(t0)), dt_obs(dt), Nt(nt),
           buf(pts.size() * (std::size_t)nt * 6, 0.0) {
         if (T0.size() != pts.size()) throw IOexception("MeshedScreen - t0 size mismatch.");
     }
+    // A triangle mesh given directly: corner points, the cells' corner
+    // indices [Np][3], and per cell the observation point and start time.
+    MeshedScreen(std::string filename, std::vector<Vector> corners, std::vector<int> triangles,
+                 std::vector<Vector> points, std::vector<double> t0, double dt, int nt)
+        : MeshedScreen(std::move(points), std::move(t0), dt, nt) {
+        FileName = std::move(filename);
+        corner = std::move(corners);
+        if (triangles.size() != 3 * pts.size())
+            throw IOexception("MeshedScreen - triangle count mismatch.");
+        tri.assign(triangles.begin(), triangles.end());
+        for (int64_t c : tri)
+            if (c < 0 || c >= (int64_t)corner.size())
+                throw IOexception("MeshedScreen - MeshTriangles index out of range");
+    }
     int get_Np() const { return (int)pts.size(); }
+    int get_Nt() const { return Nt; }
+    double get_dt() const { return dt_obs; }
     Vector get_point(int ip) const { return pts[ip]; }
     double get_t0(int ip) const { return T0[ip]; }
+    Vector get_xi(int ip) const { return xi[ip]; }
+    Vector get_eta(int ip) const { return eta[ip]; }
+    Vector get_normal(int ip) const { return normal[ip]; }
+    double get_area(int ip) const { return area[ip]; }
+    double getTotalArea() const { return total_area; }
+
+    // Cell areas, unit normals and the cell-local (xi, eta, normal) frames,
+    // as src/mesh.cpp:227-278 computes them.
+    void init() {
+        if (tri.size() != 3 * pts.size())
+            throw IOexception("MeshedScreen::init - the screen has no triangle mesh.");
+        const std::size_t np = pts.size();
+        area.assign(np, 0.0);
+        normal.assign(np, Vector());
+        xi.assign(np, Vector());
+        eta.assign(np, Vector());
+        total_area = 0.0;
+        Vector avg;
+        for (std::size_t ip = 0; ip < np; ip++) {
+            const Vector& p1 = corner[(std::size_t)tri[3 * ip]];
+            const Vector& p2 = corner[(std::size_t)tri[3 * ip + 1]];
+            const Vector& p3 = corner[(std::size_t)tri[3 * ip + 2]];
+            Vector n = cross(p3 - p1, p2 - p1);
+            area[ip] = n.norm() * 0.5;
+            total_area += area[ip];
+            n.normalize();
+            normal[ip] = n;
+            avg += n;
+        }
+        avg.normalize();
+        for (std::size_t ip = 0; ip < np; ip++) {
+            if (avg.y < 0.7) {  // xi in the x-z plane
+                xi[ip] = cross(Vector(0.0, 1.0, 0.0), normal[ip]);
+                xi[ip].normalize();
+                eta[ip] = cross(normal[ip], xi[ip]);
+                eta[ip].normalize();
+            } else {  // eta in the y-z plane
+                eta[ip] = cross(normal[ip], Vector(1.0, 0.0, 0.0));
+                eta[ip].normalize();
+                xi[ip] = cross(eta[ip], normal[ip]);
+                xi[ip].normalize();
+            }
+        }
+    }
+
+    ElMagField getField(int ip, int it) const {
+        if (ip < 0 || ip >= (int)pts.size() || it < 0 || it >= Nt)
+            throw IOexception("MeshedScreen::getField() - index out of range.");
+        ElMagField f;
+        std::memcpy(f.c, &buf[((std::size_t)ip * Nt + it) * 6], sizeof f.c);
+        return f;
+    }
+
+    // dt * sum over the trace of E x B / mu0 (FieldTrace::Poynting,
+    // src/fieldtrace.cpp:192-198)
+    Vector Poynting(int ip) const {
+        Vector sum;
+        for (int it = 0; it < Nt; it++) {
+            const double* f = &buf[((std::size_t)ip * Nt + it) * 6];
+            sum += cross(Vector(f[0], f[1], f[2]), Vector(f[3], f[4], f[5])) * (1.0 / kMuNull);
+        }
+        return sum * dt_obs;
+    }
+
+    // Energy through the screen [J], flow against the normal counted
+    // positive (src/mesh.cpp:744-754).  init() must have run.
+    double totalEnergy() const {
+        if (area.size() != pts.size())
+            throw IOexception("MeshedScreen::totalEnergy - init() has not been called.");
+        double total = 0.0;
+        for (int ip = 0; ip < (int)pts.size(); ip++) total -= area[ip] * dot(Poynting(ip), normal[ip]);
+        return total;
+    }
+
     void integrate() override {
         if (!source) throw IOexception("MeshedScreen::integrate - no source set");
+        if (Nt == 0 || pts.empty()) return;
         std::vector<double> pos(3 * pts.size());
         for (std::size_t i = 0; i < pts.size(); i++) {
             pos[3 * i] = pts[i].x;
@@ -246,19 +421,103 @@ public:
             throw IOexception("MeshedScreen::fromBuffer() - buffer size mismatch.");
         std::memcpy(buf.data(), buffer, sizeof(double) * size);
     }
-    // The reference writes HDF5 here (MeshedScreen::writeFile (src/mesh.cpp:428-736)); this build
-    // has no HDF5 library, so the traces leave through getBuffer().
-    void generateOutput() override {
-        throw IOexception("MeshedScreen::generateOutput - HDF5 output is not available in this build");
+    // The HDF5 layout of src/mesh.cpp:428-736, which the file constructor
+    // reads back: MeshCornerPoints [Ncp][3] (Ncp), ObservationPosition
+    // [Np][3] (Np), MeshTriangles [Np][3] (Ntri), ObservationTime [Np]
+    // (Nt, dt) and ElMagField [Np][Nt][6].
+    void writeFile(const std::string& filename) {
+        if (tri.size() != 3 * pts.size())
+            throw IOexception("MeshedScreen::writeFile - the screen has no triangle mesh.");
+        const uint64_t ncp = corner.size(), np = pts.size();
+        std::vector<double> cp(3 * ncp), pp(3 * np);
+        for (std::size_t i = 0; i < ncp; i++) {
+            cp[3 * i] = corner[i].x;
+            cp[3 * i + 1] = corner[i].y;
+            cp[3 * i + 2] = corner[i].z;
+        }
+        for (std::size_t i = 0; i < np; i++) {
+            pp[3 * i] = pts[i].x;
+            pp[3 * i + 1] = pts[i].y;
+            pp[3 * i + 2] = pts[i].z;
+        }
+        std::vector<int32_t> tr(tri.begin(), tri.end());
+        using h5::AttrOut;
+        try {
+            h5::Writer w;
+            w.add("MeshCornerPoints", {ncp, 3}, cp.data(), {AttrOut::Int("Ncp", (int32_t)ncp)});
+            w.add("ObservationPosition", {np, 3}, pp.data(), {AttrOut::Int("Np", (int32_t)np)});
+            w.add("MeshTriangles", {np, 3}, tr.data(), {AttrOut::Int("Ntri", (int32_t)np)});
+            w.add("ObservationTime", {np}, T0.data(),
+                  {AttrOut::Int("Nt", Nt), AttrOut::Double("dt", dt_obs)});
+            w.add("ElMagField", {np, (uint64_t)Nt, 6}, buf.data());
+            w.write(filename);
+        } catch (const h5::Error& e) {
+            throw IOexception(std::string("MeshedScreen::writeFile - ") + e.what());
+        }
     }
+    void writeFile() { writeFile(FileName); }
+    void generateOutput() override { writeFile(); }
     void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
 
 private:
+    void load(const std::string& filename) {
+        h5::File f(filename);
+        h5::Dataset d = f.dataset("MeshCornerPoints");
+        const int64_t ncp = h5::File::attr_int(d, "Ncp");
+        std::vector<double> v = f.read_double(d);
+        if (ncp < 0 || v.size() != 3 * (std::size_t)ncp)
+            throw IOexception("MeshedScreen - error reading dataset MeshCornerPoints");
+        corner.resize((std::size_t)ncp);
+        for (std::size_t i = 0; i < corner.size(); i++) corner[i] = Vector(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+
+        d = f.dataset("ObservationPosition");
+        const int64_t np = h5::File::attr_int(d, "Np");
+        v = f.read_double(d);
+        if (np < 0 || v.size() != 3 * (std::size_t)np)
+            throw IOexception("MeshedScreen - error reading dataset ObservationPosition");
+        pts.resize((std::size_t)np);
+        for (std::size_t i = 0; i < pts.size(); i++) pts[i] = Vector(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+
+        tri = f.read_int(f.dataset("MeshTriangles"));
+        if (tri.size() != 3 * pts.size())
+            throw IOexception("MeshedScreen - error reading dataset MeshTriangles");
+        for (int64_t c : tri)
+            if (c < 0 || c >= ncp) throw IOexception("MeshedScreen - MeshTriangles index out of range");
+
+        if (f.exists("ObservationTime")) {
+            d = f.dataset("ObservationTime");
+            const int64_t nt = h5::File::attr_int(d, "Nt");
+            if (nt < 0 || nt > (int64_t)1 << 30)
+                throw IOexception("MeshedScreen - error reading dataset ObservationTime attribute Nt");
+            Nt = (int)nt;
+            dt_obs = h5::File::attr_double(d, "dt");
+            T0 = f.read_double(d);
+            if (T0.size() != pts.size())
+                throw IOexception("MeshedScreen - error reading dataset ObservationTime");
+        } else {
+            Nt = 0;
+            dt_obs = 0.0;
+            T0.assign(pts.size(), 0.0);
+        }
+        buf.assign(pts.size() * (std::size_t)Nt * 6, 0.0);
+        if (f.exists("ElMagField")) {
+            v = f.read_double(f.dataset("ElMagField"));
+            if (v.size() != buf.size()) throw IOexception("MeshedScreen - error reading dataset ElMagField");
+            buf = std::move(v);
+        }
+    }
+
+    std::string FileName;
+    std::vector<Vector> corner;   // MeshCornerPoints
+    std::vector<int64_t> tri;     // [Np][3] corner indices
     std::vector<Vector> pts;
     std::vector<double> T0;
-    double dt_obs;
-    int Nt;
+    double dt_obs = 0.0;
+    int Nt = 0;
     std::vector<double> buf;  // [Np][Nt][6]
+    std::vector<Vector> xi, eta, normal;
+    std::vector<double> area;
+    double total_area = 0.0;
 };
 
 // The trace of one observation point as an SDDS (version 1) file in ASCII

@@ -210,3 +210,34 @@ def track_reference(init, lattice_packed, tstep, n_steps, charge, mass):
     if rc != 0:
         raise RuntimeError(f"ref_track failed: {rc}")
     return t, x, p, a
+
+
+def reference_file(rel: str):
+    """Path of a file of the reference tree (rel to its root), or None where
+    the tree is absent.  The tree is found beside its src/ directory."""
+    src = Path(os.environ.get("TEUFEL_REFERENCE_SRC", "/root/reference/src"))
+    f = src.parent / rel
+    return f if f.exists() else None
+
+
+MU_NULL = 4.0 * np.pi * 1e-7  # src/global.h:43
+
+
+def mesh_cells(corner, tri):
+    """Cell areas and unit normals of a triangle mesh, as MeshedScreen::init
+    computes them (src/mesh.cpp:227-247): n = (p3-p1) x (p2-p1)."""
+    p1, p2, p3 = corner[tri[:, 0]], corner[tri[:, 1]], corner[tri[:, 2]]
+    n = np.cross(p3 - p1, p2 - p1)
+    norm = np.linalg.norm(n, axis=1)
+    return 0.5 * norm, n / norm[:, None]
+
+
+def mesh_energy(corner, tri, traces, dt):
+    """(total, per-cell) energy through a meshed screen [J]: minus the cell
+    area times the time-integrated Poynting vector along the normal
+    (MeshedScreen::totalEnergy, src/mesh.cpp:744-754, with
+    FieldTrace::Poynting, src/fieldtrace.cpp:192-198)."""
+    area, normal = mesh_cells(corner, tri)
+    s = np.cross(traces[:, :, 0:3], traces[:, :, 3:6]).sum(axis=1) / MU_NULL * dt
+    flux = -area * np.einsum("ij,ij->i", s, normal)
+    return float(flux.sum()), flux

@@ -21,6 +21,10 @@ Fixtures (numpy .npz, compressed):
                       electrostatic test (tests/teufel.electrostatic.cpp:60-233:
                       a 1 pC charge at rest, and moving at gamma = 10 through a
                       field-free region) and of the single-electron undulator run
+  diffraction_screen.npz  the mesh of tests/DiffractionScreen.h5 and the
+                      reference's tracking and traces of its known-answer
+                      test (tests/teufel.DiffractionScreen.cpp:67-153): energy,
+                      per-cell energy and 8 pixels' traces
 """
 import os
 import sys
@@ -200,6 +204,41 @@ def retarded_fields(tr1):
                         **flat, **{f"geo__{k}": v for k, v in geo.items()})
 
 
+def diffraction_screen():
+    """tests/teufel.DiffractionScreen.cpp:67-153: a 100 pC macro-particle at
+    gamma = 20 tracked from z = -10 m through an empty lattice for 20000 Vay
+    steps, recorded on the annular mesh of tests/DiffractionScreen.h5 (read
+    here with the numpy HDF5 reader tests/h5min.py)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from h5min import H5Min
+    f = H5Min(str(lw.reference_file("tests/DiffractionScreen.h5")))
+    corner, ca, _ = f.dataset("MeshCornerPoints")
+    tri, ta, _ = f.dataset("MeshTriangles")
+    pos, pa, _ = f.dataset("ObservationPosition")
+    t0, oa, _ = f.dataset("ObservationTime")
+    nt, dt = int(oa["Nt"]), float(oa["dt"])
+    gamma, charge, nots = 20.0, 100e-12, 20000
+    beta = np.sqrt(1.0 - 1.0 / (gamma * gamma))
+    init = np.array([[-10.0 / (beta * C), 0.0, 0.0, -10.0, 0.0, 0.0, np.sqrt(gamma * gamma - 1.0)]])
+    tstep = 20.0 / (beta * C) / nots
+    q = charge / E_CHARGE
+    t, x, p, a = lw.track_reference(init, np.zeros(16), tstep, nots, -q, q)
+    traj = H.Trajectories(t, x, p, a, np.array([nots + 1], np.int32), np.array([-q]),
+                          np.array([q]))
+    traces, rc = lw.integrate_screen(traj, pos, t0, dt, nt, impl="reference")
+    assert rc == 0, rc
+    energy, flux = lw.mesh_energy(corner, tri.astype(np.int64), traces, dt)
+    print(f"DiffractionScreen: reference energy {energy * 1e6:.6f} uJ")
+    sel = np.argsort(flux)[::-1][:4].tolist() + [0, 300, 900, 1461]
+    check = np.arange(0, nots + 1, 1000)
+    np.savez_compressed(os.path.join(HERE, "diffraction_screen.npz"), corner=corner,
+                        tri=tri.astype(np.int32), pos=pos, t0=t0, nt=nt, dt=dt,
+                        attrs=np.array([int(ca["Ncp"]), int(ta["Ntri"]), int(pa["Np"])]),
+                        init=init, tstep=tstep, n_steps=nots, charge=-q, mass=q,
+                        check_idx=check, check_t=t[check], check_x=x[check], check_p=p[check],
+                        energy=energy, flux=flux, pix=np.array(sel), traces=traces[sel])
+
+
 def main():
     lw.build(with_reference=True)
     if not lw.reference_available():
@@ -209,6 +248,7 @@ def main():
     loop_run()
     screens(w, w2, tr1, tr4, ne)
     range_errors()
+    diffraction_screen()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

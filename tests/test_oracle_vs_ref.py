@@ -100,3 +100,28 @@ def test_oracle_equals_reference_on_config1_subset():
                                  impl="reference")
     assert rc1 == rc2 == 0
     assert np.array_equal(a, b)
+
+
+def test_diffraction_screen_kat():
+    """tests/teufel.DiffractionScreen.cpp:67-153 with the harness pusher and the
+    oracle: a 100 pC macro-particle at gamma = 20 from z = -10 m to +10 m in
+    20000 steps; the energy through the annular mesh is 0.463 +- 0.020 uJ,
+    and trajectory, per-cell energies and traces equal the reference's."""
+    d = load("diffraction_screen.npz")
+    tr = H.track(d["init"], H.Lattice(), float(d["tstep"]), int(d["n_steps"]),
+                 float(d["charge"]), float(d["mass"]))
+    idx = d["check_idx"]
+    same(tr.t[idx], d["check_t"])
+    same(tr.x[idx], d["check_x"])
+    same(tr.p[idx], d["check_p"])
+    beta = np.sqrt(1.0 - 1.0 / 400.0)
+    assert abs(tr.t[0] + 10.0 / (beta * 2.99792458e8)) < 1e-6
+    assert abs(tr.x[-1, 2] - 10.0) < 1e-6
+    dt, nt = float(d["dt"]), int(d["nt"])
+    traces, rc = lw.integrate_screen(tr, d["pos"], d["t0"], dt, nt)
+    assert rc == 0
+    energy, flux = lw.mesh_energy(d["corner"], d["tri"].astype(np.int64), traces, dt)
+    assert abs(energy * 1e6 - 0.463) <= 0.020
+    same(traces[d["pix"]], d["traces"])
+    np.testing.assert_allclose(flux, d["flux"], rtol=0, atol=1e-12 * np.abs(d["flux"]).max())
+    np.testing.assert_allclose(energy, float(d["energy"]), rtol=1e-12)
