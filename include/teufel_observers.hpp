@@ -112,6 +112,44 @@ public:
     }
     int getNOP() const { return (int)npts.size(); }
 
+    // Position and beta*gamma of particle i at a time, interpolated linearly
+    // between the bracketing trajectory points; zero outside the trajectory
+    // (ChargedParticle::CoordinatesAtTime, src/particle.cpp:514-558).
+    void CoordinatesAtTime(int i, double time, Vector* position, Vector* momentum) const {
+        std::size_t first = 0;
+        for (int k = 0; k < i; k++) first += (std::size_t)npts[k];
+        const int np = npts[i];
+        *position = Vector(0.0, 0.0, 0.0);
+        *momentum = Vector(0.0, 0.0, 0.0);
+        if (np < 1) return;
+        int i1 = 0, i2 = np - 1;
+        double t1 = T[first], t2 = T[first + i2];
+        if (!(time >= t1 && time <= t2)) return;
+        while (i2 - i1 > 1) {
+            const int im = (i2 + i1) / 2;
+            const double t = T[first + im];
+            if (t < time) {
+                i1 = im;
+                t1 = t;
+            } else {
+                i2 = im;
+                t2 = t;
+            }
+        }
+        const double* x1 = &X[3 * (first + i1)];
+        const double* p1 = &P[3 * (first + i1)];
+        if (i2 == i1) {
+            *position = Vector(x1[0], x1[1], x1[2]);
+            *momentum = Vector(p1[0], p1[1], p1[2]);
+            return;
+        }
+        const double* x2 = &X[3 * (first + i2)];
+        const double* p2 = &P[3 * (first + i2)];
+        const double frac = (time - t1) / (t2 - t1);
+        *position = Vector(x1[0], x1[1], x1[2]) * (1.0 - frac) + Vector(x2[0], x2[1], x2[2]) * frac;
+        *momentum = Vector(p1[0], p1[1], p1[2]) * (1.0 - frac) + Vector(p2[0], p2[1], p2[2]) * frac;
+    }
+
     // the device-resident set, uploaded on first use
     const teufel_traj_set* device() {
         if (!handle)
@@ -643,11 +681,56 @@ public:
             throw IOexception("SnapshotObserver::fromBuffer() - buffer size mismatch.");
         if (size) std::memcpy(buf.data(), buffer, sizeof(double) * size);
     }
-    // The reference writes HDF5 here (src/snapshot.cpp); this build has no
-    // HDF5 library, so the fields leave through getBuffer().
-    void generateOutput() override {
-        throw IOexception("SnapshotObserver::generateOutput - HDF5 output is not available in this build");
+    // Every particle's position and beta*gamma at the snapshot time, kept for
+    // the output file (src/snapshot.cpp:114-149); returns the count.
+    int storeParticlePositions() {
+        particles.clear();
+        if (!source) return particlesStored = 0;
+        const int nop = source->getNOP();
+        particles.resize(6 * (std::size_t)nop);
+        for (int i = 0; i < nop; i++) {
+            Vector x, bg;
+            source->CoordinatesAtTime(i, t_obs, &x, &bg);
+            double* q = &particles[6 * (std::size_t)i];
+            q[0] = x.x;
+            q[1] = x.y;
+            q[2] = x.z;
+            q[3] = bg.x;
+            q[4] = bg.y;
+            q[5] = bg.z;
+        }
+        return particlesStored = nop;
     }
+    const std::vector<double>& getParticleCoordinates() const { return particles; }
+
+    // The HDF5 layout of src/snapshot.cpp:226-396: ObservationPosition
+    // [Nx][Ny][3] (Nx, Ny), ElMagField [Nx][Ny][6] (t0) and, after
+    // storeParticlePositions(), ParticleCoordinates [N][6] (N_particles).
+    void WriteFieldHDF5() {
+        std::vector<double> pos((std::size_t)Nx * Ny * 3);
+        for (unsigned int ix = 0; ix < Nx; ix++)
+            for (unsigned int iy = 0; iy < Ny; iy++) {
+                const Vector c = CellPosition((int)ix, (int)iy);
+                double* q = &pos[((std::size_t)ix * Ny + iy) * 3];
+                q[0] = c.x;
+                q[1] = c.y;
+                q[2] = c.z;
+            }
+        using h5::AttrOut;
+        try {
+            h5::Writer w;
+            w.add("ObservationPosition", {Nx, Ny, 3}, pos.data(),
+                  {AttrOut::Int("Nx", (int32_t)Nx), AttrOut::Int("Ny", (int32_t)Ny)});
+            w.add("ElMagField", {Nx, Ny, 6}, buf.data(), {AttrOut::Double("t0", t_obs)});
+            if (particlesStored > 0)
+                w.add("ParticleCoordinates", {(uint64_t)particlesStored, 6}, particles.data(),
+                      {AttrOut::Int("N_particles", particlesStored)});
+            w.write(FileName);
+        } catch (const h5::Error& e) {
+            throw IOexception(std::string("SnapshotObserver::WriteFieldHDF5 - ") + e.what());
+        }
+    }
+    void generateOutput() override { WriteFieldHDF5(); }
 
 private:
     std::string FileName;
@@ -655,6 +738,8 @@ private:
     unsigned int Nx, Ny;
     double t_obs;
     std::vector<double> buf;  // [Nx][Ny][6]
+    std::vector<double> particles;  // [particlesStored][6]
+    int particlesStored = 0;
 };
 
 }  // namespace teufel_gb300

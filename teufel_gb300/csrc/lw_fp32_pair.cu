@@ -117,6 +117,7 @@ struct PointState2 {
     int fla, flb;   // window flags; kExact when resolved exactly, else 0 until materialized
     bool rega, regb;  // resolved without fallback, bin inside the trace
     V2 N;
+    F2 iR;          // 1/|R|
     F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
 };
 
@@ -150,6 +151,7 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
     const F2 iR = rsqrt2(dot(D, D));
     const V2 N = D * iR;
     S.N = N;
+    S.iR = iR;
     const V2 W = cross(b, N);
     const F2 rc1 = rcp2(one + dot(b, N));
     const F2 kappa = fma((one - eps) * dot(W, W), rc1, eps);
@@ -170,19 +172,30 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
     S.f[5] = Bv.z;
 }
 
-// step_increment for both particles; q is the pair-point the step starts at.
+// step_increment (lw_fp32_point.cuh: the exact split form of the arrival
+// increment) for both particles; q is the pair-point the step starts at.
 __device__ __forceinline__ F2 step_increment2(const PointState2& p1, const PointState2& p2,
                                               const PairPoint& q, F2 kdt) {
     const V2 ch{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])};
     const F2 ceps = hi2(q.d[7]);
     const F2 dt = hi2(q.d[1]);
-    const V2 s = p1.N + p2.N;
+    const F2 one = f2(1.0f, 1.0f), two = f2(2.0f, 2.0f);
+    const F2 rho = (p2.iR - p1.iR) * rcp2(p1.iR + p2.iR);
     const V2 d = p1.N - p2.N;
+    const V2 s0 = p1.N + p2.N;
+    const V2 s{fma(rho, d.x, s0.x), fma(rho, d.y, s0.y), fma(rho, d.z, s0.z)};
+    const F2 g = fma(f2(-rho.v.x, -rho.v.y), rho, one) * dot(d, d);
+    const F2 s2 = f2(4.0f, 4.0f) - g;
+    const F2 sn = s2 * rsqrt2(s2);
     const V2 w = cross(ch, s);
-    const F2 den = fma(f2(2.0f, 2.0f), dot(ch, s), f2(4.0f, 4.0f));
-    const F2 one_m_cos = dot(w, w) * rcp2(den);
-    const F2 one_m_n = f2(0.125f, 0.125f) * dot(d, d);
-    const F2 kap = fma(f2(1.0f, 1.0f) - ceps, one_m_n + one_m_cos, ceps);
+    const F2 bs = dot(ch, s);
+    const F2 back = sn - bs;
+    const F2 w2 = dot(w, w), b2 = back * back;
+    const F2 qq = f2(bs.v.x > 0.0f ? w2.v.x : b2.v.x, bs.v.y > 0.0f ? w2.v.y : b2.v.y);
+    const F2 a = two + sn;
+    const F2 b = sn + f2(fabsf(bs.v.x), fabsf(bs.v.y));
+    const F2 one_m_cm = fma(g, b, qq * a) * rcp2(two * a * b);
+    const F2 kap = fma(one - ceps, one_m_cm, ceps);
     return dt * kdt * kap;
 }
 

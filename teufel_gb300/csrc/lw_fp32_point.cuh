@@ -187,6 +187,7 @@ struct PointState {
     int flags;     // kLeTmin | kLtTmax | kExact
     float dt;      // duration of the trajectory step that starts at this point
     float Nx, Ny, Nz;
+    float iR;      // 1/|R|
     float2 f[3];   // (Ex, Ey), (Ez, c*Bx), (c*By, c*Bz): packed for the f32x2 pipe
 };
 
@@ -200,6 +201,7 @@ __device__ __forceinline__ void point_field(PointState& S, float4 a, float4 b, f
     S.Nx = Nx;
     S.Ny = Ny;
     S.Nz = Nz;
+    S.iR = iR;
     S.dt = a.w;
     // kappa = 1 - n.beta in split form
     const float Wx = b.y * Nz - b.z * Ny, Wy = b.z * Nx - b.x * Nz, Wz = b.x * Ny - b.y * Nx;
@@ -228,23 +230,40 @@ __device__ __forceinline__ void point_field(PointState& S, float4 a, float4 b, f
     S.f[2] = make_float2(Nz * Ex - Nx * Ez, Nx * Ey - Ny * Ex);
 }
 
-// Arrival increment of the step from point 1 to point 2 [bins]:
-//   dt (1 - |beta_c| + |beta_c| (1 - |n_m|) + |beta_c| |n_m| (1 - cos theta))
-// with n_m along N1 + N2, 1 - |n_m| = |N1 - N2|^2 / 8 to leading order, and
-// 1 - cos theta = |beta_c x s|^2 / (|s| (|s| + beta_c.s)), s = N1 + N2, |s| ~ 2
-// (|s| = 2 - |N1 - N2|^2/4, and the FP32 normalisation of N is good to 1e-7).
+// Arrival increment of the step from point 1 to point 2 [bins], in a form
+// without cancellation.  With R1, R2 the distance vectors, N = R/|R|, and the
+// chord x2 - x1 = beta_c c dt along the unit vector c^:
+//   |R1| - |R2| = (x2 - x1).(R1 + R2) / (|R1| + |R2|) = beta_c c dt (c^.m),
+//   m = w1 N1 + w2 N2,  w1,2 = |R1,2| / (|R1| + |R2|),
+// so the increment is dt (1 - |beta_c| + |beta_c| (1 - c^.m)) with
+//   1 - c^.m = (1 - |m|) + (|m| - c^.m),
+//   1 - |m|^2 = w1 w2 |N1 - N2|^2,  1 - |m| = (1 - |m|^2) / (1 + |m|),
+//   |m| - c^.m = |c^ x m|^2 / (|m| + c^.m)   when c^.m > 0, else taken directly.
+// In terms of s = 2m = N1 + N2 + rho (N1 - N2), rho = (|R1| - |R2|)/(|R1| + |R2|),
+// g = (1 - rho^2) |N1 - N2|^2 = 4 (1 - |m|^2) and |s| = sqrt(4 - g):
+//   1 - c^.m = g / (2 (2 + |s|)) + q / (2 (|s| + |c^.s|)),
+//   q = |c^ x s|^2 if c^.s > 0, else (|s| - c^.s)^2.
+// Exact for any step length and distance, so a step that passes close to the
+// observation point (near field) keeps the arrival chain to FP32 rounding.
 __device__ __forceinline__ float step_increment(const PointState& p1, const PointState& p2,
                                                 float4 chord, float kdt) {
-    const float sx = p1.Nx + p2.Nx, sy = p1.Ny + p2.Ny, sz = p1.Nz + p2.Nz;
+    const float rho = __fdividef(p2.iR - p1.iR, p1.iR + p2.iR);
     const float dx = p1.Nx - p2.Nx, dy = p1.Ny - p2.Ny, dz = p1.Nz - p2.Nz;
+    const float sx = fmaf(rho, dx, p1.Nx + p2.Nx);
+    const float sy = fmaf(rho, dy, p1.Ny + p2.Ny);
+    const float sz = fmaf(rho, dz, p1.Nz + p2.Nz);
+    const float g = fmaf(-rho, rho, 1.0f) * (dx * dx + dy * dy + dz * dz);
+    const float s2 = 4.0f - g;
+    const float sn = s2 * rsqrtf(s2);
     const float wx = chord.y * sz - chord.z * sy;
     const float wy = chord.z * sx - chord.x * sz;
     const float wz = chord.x * sy - chord.y * sx;
-    const float w2 = wx * wx + wy * wy + wz * wz;
     const float bs = chord.x * sx + chord.y * sy + chord.z * sz;
-    const float one_m_cos = __fdividef(w2, 4.0f + 2.0f * bs);
-    const float one_m_n = 0.125f * (dx * dx + dy * dy + dz * dz);
-    const float kap = chord.w + (1.0f - chord.w) * (one_m_n + one_m_cos);
+    const float back = sn - bs;
+    const float q = bs > 0.0f ? wx * wx + wy * wy + wz * wz : back * back;
+    const float a = 2.0f + sn, b = sn + fabsf(bs);
+    const float one_m_cm = __fdividef(fmaf(g, b, q * a), 2.0f * a * b);
+    const float kap = chord.w + (1.0f - chord.w) * one_m_cm;
     return p1.dt * kdt * kap;
 }
 
