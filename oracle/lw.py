@@ -93,6 +93,8 @@ def reference():
         L.ref_deposit_injected.restype = ctypes.c_int
         L.ref_deposit_injected.argtypes = [_i64, _lp, _dp, _dp, ctypes.c_double,
                                            ctypes.c_double, _i64, _dp]
+        L.ref_coordinates_at_time.restype = ctypes.c_int
+        L.ref_coordinates_at_time.argtypes = [_i64, _lp, _dp, _dp, _dp, ctypes.c_double, _dp]
         _ref = L
     return _ref
 
@@ -241,3 +243,13 @@ def mesh_energy(corner, tri, traces, dt):
     s = np.cross(traces[:, :, 0:3], traces[:, :, 3:6]).sum(axis=1) / MU_NULL * dt
     flux = -area * np.einsum("ij,ij->i", s, normal)
     return float(flux.sum()), flux
+
+
+def coordinates_at_time(traj, time):
+    """[n_particles][6] position and beta*gamma of every particle at ``time``
+    from the reference's ChargedParticle::CoordinatesAtTime."""
+    out = np.zeros((traj.n_particles, 6))
+    reference().ref_coordinates_at_time(traj.n_particles, _p(_c(traj.offsets, np.int64), _lp),
+                                        _p(_c(traj.t)), _p(_c(traj.x)), _p(_c(traj.p)), time,
+                                        _p(out))
+    return out

@@ -229,3 +229,29 @@ int ref_deposit_injected(int64_t n_part, const int64_t* offsets, const double* t
 }
 
 }  // extern "C"
+
+// The reference's ChargedParticle::CoordinatesAtTime (src/particle.cpp:514-558)
+// of every particle at one time: out[n_part][6] = position, beta*gamma.
+extern "C" int ref_coordinates_at_time(int64_t n_part, const int64_t* offsets, const double* t,
+                                       const double* x, const double* p, double time,
+                                       double* out) {
+    for (int64_t m = 0; m < n_part; m++) {
+        int64_t o = offsets[m], np = offsets[m + 1] - o;
+        std::vector<double> buf(9 + 10 * np, 0.0);
+        buf[0] = -1.0;
+        buf[1] = 1.0;
+        for (int64_t k = 0; k < np; k++) {
+            double* b = buf.data() + 9 + 10 * k;
+            b[0] = t[o + k];
+            std::memcpy(b + 1, x + 3 * (o + k), 24);
+            std::memcpy(b + 4, p + 3 * (o + k), 24);
+        }
+        ChargedParticle part(buf.data(), (int)np, 0);
+        Vector X, BG;
+        part.CoordinatesAtTime(time, &X, &BG);
+        double* q = out + 6 * m;
+        q[0] = X.x; q[1] = X.y; q[2] = X.z;
+        q[3] = BG.x; q[4] = BG.y; q[5] = BG.z;
+    }
+    return 0;
+}

@@ -9,6 +9,9 @@
 //                                            energies before and after
 //   mesh_driver screen <out.h5>              ScreenObserver::generateOutput of a
 //                                            fixed 3 x 2 x 4 screen
+//   mesh_driver snapshot <parts.bin> <t> <out.h5>
+//                                            SnapshotObserver::generateOutput with
+//                                            the particles' coordinates at t
 //   mesh_driver kat    <mesh.bin> <traj.bin> <in.h5> <out.h5>
 //                                            writeFile(in.h5), MeshedScreen(in.h5),
 //                                            init, integrate on the GPU from the
@@ -17,8 +20,10 @@
 // mesh.bin: int32 ncp, np, nt; double dt; double corner[ncp][3]; int32
 // tri[np][3]; double pos[np][3]; double t0[np]; double field[np][nt][6].
 // traj.bin: int32 n; double charge [C]; double t[n], x[n][3], p[n][3], a[n][3].
+// parts.bin: int32 count, then count records in the traj.bin format.
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <stdexcept>
@@ -146,6 +151,32 @@ int cmd_screen(const char* h5) {
     return 0;
 }
 
+// traj.bin particles (trajectory format above, n points each, count given by
+// the file), a 4 x 3 snapshot at time t with ramp fields, particle coordinates
+// stored, written by generateOutput().
+int cmd_snapshot(const char* traj, double t, const char* h5) {
+    Reader r(traj);
+    const int nop = r.get<int32_t>(1)[0];
+    TrajectorySource src;
+    for (int m = 0; m < nop; m++) {
+        const int n = r.get<int32_t>(1)[0];
+        const double charge = r.get<double>(1)[0];
+        const std::vector<double> tt = r.get<double>((std::size_t)n), x = r.get<double>(3 * (std::size_t)n),
+                                  p = r.get<double>(3 * (std::size_t)n), a = r.get<double>(3 * (std::size_t)n);
+        src.Add(charge, n, tt.data(), x.data(), p.data(), a.data());
+    }
+    SnapshotObserver snap(h5, Vector(0.0, 0.1, 3.0), Vector(0.002, 0.0, 0.0), Vector(0.0, 0.003, 0.0),
+                          4, 3, t);
+    snap.setSource(&src);
+    std::vector<double> f(snap.getBufferSize());
+    for (std::size_t i = 0; i < f.size(); i++) f[i] = 1.5 * (double)i + 0.25;
+    snap.fromBuffer(f.data(), f.size());
+    const int stored = snap.storeParticlePositions();
+    snap.generateOutput();
+    std::printf("stored %d\n", stored);
+    return 0;
+}
+
 int cmd_kat(const char* in, const char* traj, const char* h5_in, const char* h5_out) {
     const Mesh m = read_mesh(in);
     {
@@ -180,6 +211,7 @@ int main(int argc, char** argv) {
         if (c == "read" && argc == 4) return cmd_read(argv[2], argv[3]);
         if (c == "write" && argc == 4) return cmd_write(argv[2], argv[3]);
         if (c == "screen" && argc == 3) return cmd_screen(argv[2]);
+        if (c == "snapshot" && argc == 5) return cmd_snapshot(argv[2], std::atof(argv[3]), argv[4]);
         if (c == "kat" && argc == 6) return cmd_kat(argv[2], argv[3], argv[4], argv[5]);
         std::fprintf(stderr, "usage: mesh_driver read|write|screen|kat ...\n");
         return 2;

@@ -183,3 +183,58 @@ def test_reader_rejects_bad_files(driver, mesh, tmp_path):
         r = subprocess.run([driver, "read", str(bad), str(tmp_path / "x.bin")], capture_output=True,
                            text=True)
         assert r.returncode == 3 and "MeshedScreen - HDF5 reader" in r.stderr, (name, r.stderr)
+
+
+def test_snapshot_writer_with_particle_coordinates(driver, tmp_path):
+    """SnapshotObserver::WriteFieldHDF5 (src/snapshot.cpp:226-396) after
+    storeParticlePositions (src/snapshot.cpp:114-149): ParticleCoordinates
+    from CoordinatesAtTime (src/particle.cpp:514-558), pinned to the
+    reference's own function where its build is present."""
+    from teufel_gb300 import harness as H
+    rng = np.random.default_rng(5)
+    lens = [40, 1, 25]
+    t_snap = 2.2e-10
+    parts = tmp_path / "parts.bin"
+    ts, xs, ps = [], [], []
+    with open(parts, "wb") as fh:
+        np.array([len(lens)], np.int32).tofile(fh)
+        for m, n in enumerate(lens):
+            t = np.cumsum(rng.uniform(5e-12, 2e-11, n)) + 1e-10 * m
+            x, p, a = (rng.standard_normal((n, 3)) for _ in range(3))
+            np.array([n], np.int32).tofile(fh)
+            np.array([-1.6e-19]).tofile(fh)
+            for v in (t, x, p, a):
+                v.tofile(fh)
+            ts.append(t), xs.append(x), ps.append(p)
+    out = tmp_path / "snap.h5"
+    r = subprocess.run([driver, "snapshot", str(parts), repr(t_snap), str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    f = H5Min(str(out))
+    assert sorted(f.links) == ["ElMagField", "ObservationPosition", "ParticleCoordinates"]
+    pos, at, _ = f.dataset("ObservationPosition")
+    ix, iy = np.meshgrid(np.arange(4) - 1.5, np.arange(3) - 1.0, indexing="ij")
+    want = (np.array([0.0, 0.1, 3.0]) + np.array([0.002, 0, 0]) * ix[..., None] +
+            np.array([0, 0.003, 0]) * iy[..., None])
+    np.testing.assert_array_equal(pos, want)
+    assert {k: int(v) for k, v in at.items()} == {"Nx": 4, "Ny": 3}
+    fld, at, _ = f.dataset("ElMagField")
+    np.testing.assert_array_equal(fld, (1.5 * np.arange(72) + 0.25).reshape(4, 3, 6))
+    assert float(at["t0"]) == t_snap
+    pc, at, _ = f.dataset("ParticleCoordinates")
+    assert int(at["N_particles"]) == 3 and pc.shape == (3, 6)
+    for m in range(3):  # restated: linear interpolation inside, zero outside
+        t, x, p = ts[m], xs[m], ps[m]
+        if t[0] <= t_snap <= t[-1]:
+            i2 = max(int(np.searchsorted(t, t_snap)), 1)
+            fr = (t_snap - t[i2 - 1]) / (t[i2] - t[i2 - 1])
+            expect = np.concatenate([x[i2 - 1] * (1 - fr) + x[i2] * fr,
+                                     p[i2 - 1] * (1 - fr) + p[i2] * fr])
+        else:
+            expect = np.zeros(6)
+        np.testing.assert_allclose(pc[m], expect, rtol=1e-15, atol=0)
+    if lw.reference_available():
+        traj = H.Trajectories(np.concatenate(ts), np.concatenate(xs), np.concatenate(ps),
+                              np.zeros((sum(lens), 3)), np.array(lens, np.int32),
+                              np.full(3, -1.0), np.ones(3))
+        assert np.array_equal(pc, lw.coordinates_at_time(traj, t_snap))
