@@ -116,8 +116,8 @@ struct PointState2 {
     int idxa, idxb; // bin indices (general path only)
     int fla, flb;   // window flags; kExact when resolved exactly, else 0 until materialized
     bool rega, regb;  // resolved without fallback, bin inside the trace
-    V2 N;
     F2 iR;          // 1/|R|
+    F2 aplus;       // 1 - c^.N with c^ the chord of the step this point starts
     F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
 };
 
@@ -138,9 +138,24 @@ __device__ __forceinline__ Anchor2 pack_anchor(const Anchor& a, const Anchor& b)
     return A;
 }
 
-// point_field (lw_fp32_point.cuh) for both particles at once.
+// 1 - c^.N for a unit chord direction c^, without cancellation: |c^ x N|^2 /
+// (1 + c^.N) when c^.N > 0, else directly.
+__device__ __forceinline__ F2 one_minus_cn(const V2& ch, const V2& N) {
+    const F2 one = f2(1.0f, 1.0f);
+    const V2 x = cross(ch, N);
+    const F2 cn = dot(ch, N);
+    const F2 fwd = dot(x, x) * rcp2(one + cn);
+    const F2 back = one - cn;
+    return f2(cn.v.x > 0.0f ? fwd.v.x : back.v.x, cn.v.y > 0.0f ? fwd.v.y : back.v.y);
+}
+
+// point_field (lw_fp32_point.cuh) for both particles at once, plus the point's
+// share of the arrival increments (step_increment2): 1 - c^.N for the chord
+// of the step that ends here (qprev's chord, returned in aminus) and of the
+// step that starts here (q's chord, kept in S.aplus).
 __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
-                                             const Anchor2& A) {
+                                             const PairPoint& qprev, const Anchor2& A,
+                                             F2& aminus) {
     const V2 e{lo2(q.d[0]), hi2(q.d[0]), lo2(q.d[1])};
     const V2 b{lo2(q.d[2]), hi2(q.d[2]), lo2(q.d[3])};
     const F2 eps = hi2(q.d[3]);
@@ -150,8 +165,9 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
     const V2 D = A.D - e;
     const F2 iR = rsqrt2(dot(D, D));
     const V2 N = D * iR;
-    S.N = N;
     S.iR = iR;
+    S.aplus = one_minus_cn(V2{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])}, N);
+    aminus = one_minus_cn(V2{lo2(qprev.d[6]), hi2(qprev.d[6]), lo2(qprev.d[7])}, N);
     const V2 W = cross(b, N);
     const F2 rc1 = rcp2(one + dot(b, N));
     const F2 kappa = fma((one - eps) * dot(W, W), rc1, eps);
@@ -172,30 +188,18 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
     S.f[5] = Bv.z;
 }
 
-// step_increment (lw_fp32_point.cuh: the exact split form of the arrival
-// increment) for both particles; q is the pair-point the step starts at.
+// The arrival increment of the step from point 1 to point 2 [bins] for both
+// particles: step_increment (lw_fp32_point.cuh) with the points' shares
+// 1 - c^.N formed when each point was evaluated (point_field2), so a point
+// state carries two numbers instead of N.  q is the pair-point the step
+// starts at (its chord and dt).
 __device__ __forceinline__ F2 step_increment2(const PointState2& p1, const PointState2& p2,
-                                              const PairPoint& q, F2 kdt) {
-    const V2 ch{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])};
+                                              F2 aminus, const PairPoint& q, F2 kdt) {
     const F2 ceps = hi2(q.d[7]);
     const F2 dt = hi2(q.d[1]);
-    const F2 one = f2(1.0f, 1.0f), two = f2(2.0f, 2.0f);
-    const F2 rho = (p2.iR - p1.iR) * rcp2(p1.iR + p2.iR);
-    const V2 d = p1.N - p2.N;
-    const V2 s0 = p1.N + p2.N;
-    const V2 s{fma(rho, d.x, s0.x), fma(rho, d.y, s0.y), fma(rho, d.z, s0.z)};
-    const F2 g = fma(f2(-rho.v.x, -rho.v.y), rho, one) * dot(d, d);
-    const F2 s2 = f2(4.0f, 4.0f) - g;
-    const F2 sn = s2 * rsqrt2(s2);
-    const V2 w = cross(ch, s);
-    const F2 bs = dot(ch, s);
-    const F2 back = sn - bs;
-    const F2 w2 = dot(w, w), b2 = back * back;
-    const F2 qq = f2(bs.v.x > 0.0f ? w2.v.x : b2.v.x, bs.v.y > 0.0f ? w2.v.y : b2.v.y);
-    const F2 a = two + sn;
-    const F2 b = sn + f2(fabsf(bs.v.x), fabsf(bs.v.y));
-    const F2 one_m_cm = fma(g, b, qq * a) * rcp2(two * a * b);
-    const F2 kap = fma(one - ceps, one_m_cm, ceps);
+    const F2 t = rcp2(p1.iR + p2.iR);
+    const F2 one_m_cm = fma(p2.iR * t, p1.aplus, p1.iR * t * aminus);
+    const F2 kap = fma(f2(1.0f, 1.0f) - ceps, one_m_cm, ceps);
     return dt * kdt * kap;
 }
 
@@ -565,13 +569,14 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             // state is never copied.
             auto step = [&](PointState2& q1, PointState2& q2, int l) {
                 const int i = p0 + l;
-                point_field2(q2, B.p[l + 1], A);
+                F2 aminus;
+                point_field2(q2, B.p[l + 1], B.p[l], A, aminus);
                 if (l == 0 && anchor) {
                     start_chain2(q2, A);
                     comp = f2(0.0f, 0.0f);
                     chain_err = A.err;
                 } else {
-                    const F2 du = step_increment2(q1, q2, B.p[l], f2(px.kdt, px.kdt));
+                    const F2 du = step_increment2(q1, q2, aminus, B.p[l], f2(px.kdt, px.kdt));
                     chain_step2(q1, q2, du, comp);
                     chain_err = fma(f2(fabsf(du.v.x), fabsf(du.v.y)),
                                     f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));

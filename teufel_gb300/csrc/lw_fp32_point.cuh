@@ -230,39 +230,31 @@ __device__ __forceinline__ void point_field(PointState& S, float4 a, float4 b, f
     S.f[2] = make_float2(Nz * Ex - Nx * Ez, Nx * Ey - Ny * Ex);
 }
 
-// Arrival increment of the step from point 1 to point 2 [bins], in a form
-// without cancellation.  With R1, R2 the distance vectors, N = R/|R|, and the
-// chord x2 - x1 = beta_c c dt along the unit vector c^:
+// 1 - c^.N for unit vectors, without cancellation: |c^ x N|^2 / (1 + c^.N)
+// when c^.N > 0, else directly.
+__device__ __forceinline__ float one_minus_cn(float cx, float cy, float cz, float Nx, float Ny,
+                                              float Nz) {
+    const float wx = cy * Nz - cz * Ny, wy = cz * Nx - cx * Nz, wz = cx * Ny - cy * Nx;
+    const float cn = cx * Nx + cy * Ny + cz * Nz;
+    return cn > 0.0f ? __fdividef(wx * wx + wy * wy + wz * wz, 1.0f + cn) : 1.0f - cn;
+}
+
+// Arrival increment of the step from point 1 to point 2 [bins].  With R1, R2
+// the distance vectors, N = R/|R| and the chord x2 - x1 = beta_c c dt along
+// the unit vector c^:
 //   |R1| - |R2| = (x2 - x1).(R1 + R2) / (|R1| + |R2|) = beta_c c dt (c^.m),
-//   m = w1 N1 + w2 N2,  w1,2 = |R1,2| / (|R1| + |R2|),
-// so the increment is dt (1 - |beta_c| + |beta_c| (1 - c^.m)) with
-//   1 - c^.m = (1 - |m|) + (|m| - c^.m),
-//   1 - |m|^2 = w1 w2 |N1 - N2|^2,  1 - |m| = (1 - |m|^2) / (1 + |m|),
-//   |m| - c^.m = |c^ x m|^2 / (|m| + c^.m)   when c^.m > 0, else taken directly.
-// In terms of s = 2m = N1 + N2 + rho (N1 - N2), rho = (|R1| - |R2|)/(|R1| + |R2|),
-// g = (1 - rho^2) |N1 - N2|^2 = 4 (1 - |m|^2) and |s| = sqrt(4 - g):
-//   1 - c^.m = g / (2 (2 + |s|)) + q / (2 (|s| + |c^.s|)),
-//   q = |c^ x s|^2 if c^.s > 0, else (|s| - c^.s)^2.
-// Exact for any step length and distance, so a step that passes close to the
-// observation point (near field) keeps the arrival chain to FP32 rounding.
+//   m = (R1 + R2) / (|R1| + |R2|),
+// so the increment is dt (1 - |beta_c| + |beta_c| (1 - c^.m)), and since
+// (|R1| + |R2|)(1 - c^.m) = |R1| (1 - c^.N1) + |R2| (1 - c^.N2),
+//   1 - c^.m = w1 (1 - c^.N1) + w2 (1 - c^.N2),  w1,2 = |R1,2| / (|R1| + |R2|):
+// a weighted sum of non-negative terms, exact to rounding for any step length
+// and distance (a step that passes close to the observation point included).
 __device__ __forceinline__ float step_increment(const PointState& p1, const PointState& p2,
                                                 float4 chord, float kdt) {
-    const float rho = __fdividef(p2.iR - p1.iR, p1.iR + p2.iR);
-    const float dx = p1.Nx - p2.Nx, dy = p1.Ny - p2.Ny, dz = p1.Nz - p2.Nz;
-    const float sx = fmaf(rho, dx, p1.Nx + p2.Nx);
-    const float sy = fmaf(rho, dy, p1.Ny + p2.Ny);
-    const float sz = fmaf(rho, dz, p1.Nz + p2.Nz);
-    const float g = fmaf(-rho, rho, 1.0f) * (dx * dx + dy * dy + dz * dz);
-    const float s2 = 4.0f - g;
-    const float sn = s2 * rsqrtf(s2);
-    const float wx = chord.y * sz - chord.z * sy;
-    const float wy = chord.z * sx - chord.x * sz;
-    const float wz = chord.x * sy - chord.y * sx;
-    const float bs = chord.x * sx + chord.y * sy + chord.z * sz;
-    const float back = sn - bs;
-    const float q = bs > 0.0f ? wx * wx + wy * wy + wz * wz : back * back;
-    const float a = 2.0f + sn, b = sn + fabsf(bs);
-    const float one_m_cm = __fdividef(fmaf(g, b, q * a), 2.0f * a * b);
+    const float t = __fdividef(1.0f, p1.iR + p2.iR);
+    const float a1 = one_minus_cn(chord.x, chord.y, chord.z, p1.Nx, p1.Ny, p1.Nz);
+    const float a2 = one_minus_cn(chord.x, chord.y, chord.z, p2.Nx, p2.Ny, p2.Nz);
+    const float one_m_cm = fmaf(p2.iR * t, a1, p1.iR * t * a2);
     const float kap = chord.w + (1.0f - chord.w) * one_m_cm;
     return p1.dt * kdt * kap;
 }
