@@ -314,10 +314,12 @@ struct PairSink {
         }
     }
     // Regular steps of both particles: fa/fb say which particle deposits
-    // (its fields are zero otherwise), ka/kb its bin, sa/sb whether the step
-    // crosses into bin k+1.
+    // (its weights are zero otherwise), ka/kb its bin, sa/sb whether the step
+    // crosses into bin k+1.  Bin k receives f1 a1 + f2 b1, bin k+1 (on a
+    // crossing) f1 a2 + f2 b2, fused into the accumulators.
     __device__ __forceinline__ void add_fast(bool fa, bool fb, int ka, int kb, bool sa, bool sb,
-                                             const F2* f1, const F2* f2v) {
+                                             const F2* f1, const F2* f2v, F2 a1, F2 b1, F2 a2,
+                                             F2 b2) {
         // a bin other than the open one: only after a general-path step or at
         // the start of a walk, so one branch for both particles
         const bool na = fa && ka != open_a, nb = fb && kb != open_b;
@@ -336,7 +338,7 @@ struct PairSink {
             }
         }
 #pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = acc[c] + f1[c];
+        for (int c = 0; c < 6; c++) acc[c] = fma(f2v[c], b1, fma(f1[c], a1, acc[c]));
         // a step that crosses into the next bin closes its bin: predicated
         // reductions, no divergent branch
         reduce_if<0>(sa, ka);
@@ -345,7 +347,7 @@ struct PairSink {
         open_b = sb ? kb + 1 : open_b;
         const F2 keep = f2(sa ? 0.0f : 1.0f, sb ? 0.0f : 1.0f);
 #pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, f2v[c]);
+        for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, fma(f2v[c], b2, f1[c] * a2));
         n_add += (unsigned)fa + (unsigned)fb + (unsigned)sa + (unsigned)sb;
     }
     template <int W>
@@ -365,25 +367,28 @@ struct PairView {
 };
 
 // Regular steps of both particles (deposit_fast, lw_fp32_point.cuh, in packed
-// form).  fa/fb: the particle deposits a regular step.
+// form).  fa/fb: the particle deposits a regular step.  The step's trapezoid
+// (fields f1, f2 at arrival r1 < r2 [bins]) is split at the bin edge when it
+// crosses one: with dts = r2 - r1 (+1 on a crossing), a the part in bin k
+// (dts when no crossing), lam = a/dts and fe = (1 - lam) f1 + lam f2,
+//   bin k:   (f1 + fe) a/2       = f1 (2 - lam) a/2       + f2 lam a/2,
+//   bin k+1: (fe + f2) (dts-a)/2 = f1 (1 - lam) (dts-a)/2 + f2 (1 + lam) (dts-a)/2.
 __device__ __forceinline__ void deposit_fast2(const PointState2& p1, const PointState2& p2,
                                               int Ba, int Bb, bool fa, bool fb, PairSink& sink) {
     const bool sa = fa && p2.ka != p1.ka, sb = fb && p2.kb != p1.kb;
     const F2 dts = f2(sa ? 1.0f : 0.0f, sb ? 1.0f : 0.0f) + (p2.r - p1.r);
     const F2 h = f2(0.5f, 0.5f) - p1.r;
     const F2 a = f2(sa ? h.v.x : dts.v.x, sb ? h.v.y : dts.v.y);
-    const F2 rd = rcp2(dts);
-    const F2 lam = f2(sa ? a.v.x * rd.v.x : 1.0f, sb ? a.v.y * rd.v.y : 1.0f);
-    const F2 w1 = f2(fa ? 0.5f * a.v.x : 0.0f, fb ? 0.5f * a.v.y : 0.0f);
-    const F2 w2 = f2(0.5f, 0.5f) * (dts - a) * f2(sa ? 1.0f : 0.0f, sb ? 1.0f : 0.0f);
-    F2 field1[6], field2[6];
-#pragma unroll
-    for (int c = 0; c < 6; c++) {
-        const F2 fe = fma(p2.f[c] - p1.f[c], lam, p1.f[c]);
-        field1[c] = (p1.f[c] + fe) * w1;
-        field2[c] = (fe + p2.f[c]) * w2;
-    }
-    sink.add_fast(fa, fb, Ba + p1.ka, Bb + p1.kb, sa, sb, field1, field2);
+    // lam = 1 without a crossing: dts may be zero there (a particle past its
+    // last point repeats it)
+    const F2 q = a * rcp2(dts);
+    const F2 lam = f2(sa ? q.v.x : 1.0f, sb ? q.v.y : 1.0f);
+    const F2 hw1 = f2(fa ? 0.5f * a.v.x : 0.0f, fb ? 0.5f * a.v.y : 0.0f);
+    const F2 hw2 = f2(0.5f, 0.5f) * (dts - a);  // zero without a crossing
+    const F2 one = f2(1.0f, 1.0f);
+    const F2 a1 = (f2(2.0f, 2.0f) - lam) * hw1, b1 = lam * hw1;
+    const F2 a2 = (one - lam) * hw2, b2 = (one + lam) * hw2;
+    sink.add_fast(fa, fb, Ba + p1.ka, Bb + p1.kb, sa, sb, p1.f, p2.f, a1, b1, a2, b2);
 }
 
 // ---------------------------------------------------------------------------
