@@ -70,17 +70,6 @@ __global__ void prep_particles_kernel(DevTraj tr, double4_32a* vhat) {
     vhat[m] = v;
 }
 
-// v <- R v in the set's frame (FP64)
-__device__ __forceinline__ void to_frame(const Frame& F, double& x, double& y, double& z) {
-    if (F.identity) return;
-    const double a = fma(F.r[0], x, fma(F.r[1], y, F.r[2] * z));
-    const double b = fma(F.r[3], x, fma(F.r[4], y, F.r[5] * z));
-    const double c = fma(F.r[6], x, fma(F.r[7], y, F.r[8] * z));
-    x = a;
-    y = b;
-    z = c;
-}
-
 __global__ void prep_points_kernel(DevTraj tr, float4* q0, float4* q1, float4* q2, float4* q3) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= tr.n_points) return;

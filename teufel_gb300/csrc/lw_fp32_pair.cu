@@ -23,6 +23,43 @@ namespace teufel {
 // ---------------------------------------------------------------------------
 // Preparation: the interleaved per-point data of every pair.
 // ---------------------------------------------------------------------------
+// A pair-point is kPairPoint float4, the two particles interleaved component
+// by component (lo/hi halves: particle a, b):
+//   0-1  e (offset from the segment's first point), dt of the step it starts
+//   2-3  beta^, 1 - |beta|
+//   4-5  scaled beta', velocity-field scale
+//   6-7  dA = beta^_i - c^_i, 1 - |beta_c|   (c^_i: chord of the step i -> i+1)
+//   8-9  dB = beta^_(i+1) - c^_i, unused
+// all in the set's frame.  dA and dB give the arrival-increment shares
+// 1 - c^.N = (1 - beta^.N) + d.N of the step's two end points from the field's
+// own 1 - beta^.N; they are formed in FP64, so their FP32 values carry full
+// relative precision however small they are.
+// dA, dB of point k of a particle with points [o, o + n), in the set's frame
+__device__ __forceinline__ void chord_offsets(const DevTraj& tr, int64_t o, int64_t n, int64_t k,
+                                              double3& dA, double3& dB) {
+    auto bhat = [&](int64_t q) {
+        const double4_32a bg = tr.pp[q];
+        const double P = sqrt(bg.x * bg.x + bg.y * bg.y + bg.z * bg.z);
+        return P > 0.0 ? make_double3(bg.x / P, bg.y / P, bg.z / P) : make_double3(0.0, 0.0, 1.0);
+    };
+    double3 c = make_double3(0.0, 0.0, 1.0);
+    const double3 b1 = bhat(k);
+    double3 b2 = b1;
+    if (k + 1 < o + n) {
+        const double4_32a p = tr.tx[k], q = tr.tx[k + 1];
+        const double ex = q.y - p.y, ey = q.z - p.z, ez = q.w - p.w;
+        const double L = sqrt(ex * ex + ey * ey + ez * ez);
+        if (L > 0.0) c = make_double3(ex / L, ey / L, ez / L);
+        b2 = bhat(k + 1);
+    } else {
+        c = b1;  // no step starts at the last point
+    }
+    dA = make_double3(b1.x - c.x, b1.y - c.y, b1.z - c.z);
+    dB = make_double3(b2.x - c.x, b2.y - c.y, b2.z - c.z);
+    to_frame(tr.frame, dA.x, dA.y, dA.z);
+    to_frame(tr.frame, dB.x, dB.y, dB.z);
+}
+
 __global__ void prep_pairs_kernel(DevTraj tr, float4* pq) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total = tr.pair_offsets[tr.n_pairs];
@@ -38,27 +75,34 @@ __global__ void prep_pairs_kernel(DevTraj tr, float4* pq) {
     const int64_t oa = tr.offsets[ma], na = tr.offsets[ma + 1] - oa;
     const int64_t ob = tr.offsets[mb], nb = tr.offsets[mb + 1] - ob;
     float4 a0, a1, a2, a3, b0, b1, b2, b3;
+    double3 dAa = make_double3(0.0, 0.0, 0.0), dBa = dAa, dAb = dAa, dBb = dAa;
     if (na > 0) {
         const int64_t k = oa + (l < na ? l : na - 1);
         a0 = tr.q0[k]; a1 = tr.q1[k]; a2 = tr.q2[k]; a3 = tr.q3[k];
+        chord_offsets(tr, oa, na, k, dAa, dBa);
     } else {
         a0 = a1 = a2 = a3 = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
     }
     if (nb > 0) {
         const int64_t k = ob + (l < nb ? l : nb - 1);
         b0 = tr.q0[k]; b1 = tr.q1[k]; b2 = tr.q2[k]; b3 = tr.q3[k];
+        chord_offsets(tr, ob, nb, k, dAb, dBb);
     } else {
         b0 = a0; b1 = a1; b2 = a2; b3 = a3;
+        dAb = dAa;
+        dBb = dBa;
     }
-    float4* o = pq + 8 * i;
+    float4* o = pq + kPairPoint * i;
     o[0] = make_float4(a0.x, b0.x, a0.y, b0.y);
     o[1] = make_float4(a0.z, b0.z, a0.w, b0.w);
     o[2] = make_float4(a1.x, b1.x, a1.y, b1.y);
     o[3] = make_float4(a1.z, b1.z, a1.w, b1.w);
     o[4] = make_float4(a2.x, b2.x, a2.y, b2.y);
     o[5] = make_float4(a2.z, b2.z, a2.w, b2.w);
-    o[6] = make_float4(a3.x, b3.x, a3.y, b3.y);
-    o[7] = make_float4(a3.z, b3.z, a3.w, b3.w);
+    o[6] = make_float4((float)dAa.x, (float)dAb.x, (float)dAa.y, (float)dAb.y);
+    o[7] = make_float4((float)dAa.z, (float)dAb.z, a3.w, b3.w);
+    o[8] = make_float4((float)dBa.x, (float)dBb.x, (float)dBa.y, (float)dBb.y);
+    o[9] = make_float4((float)dBa.z, (float)dBb.z, 0.0f, 0.0f);
 }
 
 cudaError_t launch_prep_pairs(const DevTraj& tr, cudaStream_t s) {
@@ -103,9 +147,9 @@ __device__ __forceinline__ V2 operator-(const V2& a, const V2& b) {
 }
 __device__ __forceinline__ V2 operator*(const V2& a, F2 s) { return V2{a.x * s, a.y * s, a.z * s}; }
 
-// The 8 float4 of one pair-point, as staged in shared memory.
+// The kPairPoint float4 of one pair-point, as staged in shared memory.
 struct PairPoint {
-    float4 d[8];
+    float4 d[kPairPoint];
 };
 __device__ __forceinline__ F2 lo2(float4 v) { return f2(v.x, v.y); }
 __device__ __forceinline__ F2 hi2(float4 v) { return f2(v.z, v.w); }
@@ -138,21 +182,10 @@ __device__ __forceinline__ Anchor2 pack_anchor(const Anchor& a, const Anchor& b)
     return A;
 }
 
-// 1 - c^.N for a unit chord direction c^, without cancellation: |c^ x N|^2 /
-// (1 + c^.N) when c^.N > 0, else directly.
-__device__ __forceinline__ F2 one_minus_cn(const V2& ch, const V2& N) {
-    const F2 one = f2(1.0f, 1.0f);
-    const V2 x = cross(ch, N);
-    const F2 cn = dot(ch, N);
-    const F2 fwd = dot(x, x) * rcp2(one + cn);
-    const F2 back = one - cn;
-    return f2(cn.v.x > 0.0f ? fwd.v.x : back.v.x, cn.v.y > 0.0f ? fwd.v.y : back.v.y);
-}
-
 // point_field (lw_fp32_point.cuh) for both particles at once, plus the point's
-// share of the arrival increments (step_increment2): 1 - c^.N for the chord
-// of the step that ends here (qprev's chord, returned in aminus) and of the
-// step that starts here (q's chord, kept in S.aplus).
+// shares of the arrival increments (step_increment2): 1 - c^.N for the chord
+// of the step that ends here (from qprev's dB, returned in aminus) and of the
+// step that starts here (from q's dA, kept in S.aplus), as 1 - beta^.N + d.N.
 __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
                                              const PairPoint& qprev, const Anchor2& A,
                                              F2& aminus) {
@@ -166,11 +199,12 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
     const F2 iR = rsqrt2(dot(D, D));
     const V2 N = D * iR;
     S.iR = iR;
-    S.aplus = one_minus_cn(V2{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])}, N);
-    aminus = one_minus_cn(V2{lo2(qprev.d[6]), hi2(qprev.d[6]), lo2(qprev.d[7])}, N);
     const V2 W = cross(b, N);
     const F2 rc1 = rcp2(one + dot(b, N));
-    const F2 kappa = fma((one - eps) * dot(W, W), rc1, eps);
+    const F2 a0 = dot(W, W) * rc1;  // 1 - beta^.N
+    const F2 kappa = fma(one - eps, a0, eps);
+    S.aplus = a0 + dot(V2{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])}, N);
+    aminus = a0 + dot(V2{lo2(qprev.d[8]), hi2(qprev.d[8]), lo2(qprev.d[9])}, N);
     const V2 Sv = N + b;
     const V2 T = cross(W, Sv);
     const V2 mb{fma(T.x, rc1, b.x * eps), fma(T.y, rc1, b.y * eps), fma(T.z, rc1, b.z * eps)};
@@ -396,22 +430,30 @@ __device__ __forceinline__ void deposit_fast2(const PointState2& p1, const Point
 // ---------------------------------------------------------------------------
 constexpr int kPThreads = kPairTile;  // one warp per block: residency is set by registers alone
 
+// Chunks of 16 pair-points: two staged chunks and the lanes' pixel data stay
+// within 10 KB per block, so 16 one-warp blocks fit an SM's shared memory.
+// Anchors may move at chunk boundaries; segment boundaries stay chunk
+// boundaries.
+constexpr int kPChunkShift = 4;
+constexpr int kPChunkLen = 1 << kPChunkShift;
+static_assert(kSegLen % kPChunkLen == 0 && kPChunkLen % 2 == 0, "chunk layout");
+
 // A staged chunk: p[0] is the pair-point before the chunk (the start of the
 // chunk's first step), p[1 + l] the chunk's point l.
 struct __align__(16) PairChunk {
-    PairPoint p[kChunkLen + 1];
+    PairPoint p[kPChunkLen + 1];
 };
 
 // The 32 lanes copy pair-points p0-1 .. p0+avail-1 of the pair whose data
 // starts at pq (p[0] only when p0 > 0).
 __device__ __forceinline__ void pair_stage(PairChunk* b, const float4* pq, int p0, int avail,
                                            int lane) {
-    const int skip = p0 > 0 ? 0 : 8;  // float4s of p[0] not copied
-    const int n = 8 * (avail + 1);
-    const float4* src = pq + 8 * ((int64_t)p0 - 1);
+    const int skip = p0 > 0 ? 0 : kPairPoint;  // float4s of p[0] not copied
+    const int n = kPairPoint * (avail + 1);
+    const float4* src = pq + kPairPoint * ((int64_t)p0 - 1);
     float4* dst = reinterpret_cast<float4*>(b->p);
 #pragma unroll
-    for (int k = 0; k < (8 * (kChunkLen + 1) + 31) / 32; k++) {
+    for (int k = 0; k < (kPairPoint * (kPChunkLen + 1) + 31) / 32; k++) {
         const int t = lane + 32 * k;
         if (t >= skip && t < n) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + t);
@@ -514,13 +556,13 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         if (!active) lim_a = lim_b = -1;
         const int lo = warp_min(min(fa, fb)), hi = warp_max(max(la, lb));
         if (lo > hi) continue;  // uniform over the warp
-        const int start = lo & ~(kChunkLen - 1);  // >= st_lo, a segment boundary
+        const int start = lo & ~(kPChunkLen - 1);  // >= st_lo, a segment boundary
         const int64_t po = tr.pair_offsets[j];
         const unsigned int lanes = __popc(__ballot_sync(0xffffffffu, active));
         if (lane == 0) {
             W.txa = tr.tx + tr.offsets[ma];
             W.txb = tr.tx + tr.offsets[mb];
-            W.pq = tr.pq + 8 * po;
+            W.pq = tr.pq + kPairPoint * po;
             W.npa = npa;
             W.npb = npb;
             W.npp = (int)(tr.pair_offsets[j + 1] - po);
@@ -528,17 +570,17 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             sh.stats[0] += (unsigned long long)(hi + 2 - start) * (hasb ? 2u : 1u) * lanes;
         }
         __syncwarp();
-        pair_stage(&wb[0], W.pq, start, min(kChunkLen, W.npp - start), lane);
+        pair_stage(&wb[0], W.pq, start, min(kPChunkLen, W.npp - start), lane);
         Anchor2 A;
         PointState2 p1, p2;
         F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);  // chain_err includes A.err
         p2.rega = p2.regb = false;
-        const int n_chunks = (W.n_pts + kChunkLen - 1) >> kChunkShift;
+        const int n_chunks = (W.n_pts + kPChunkLen - 1) >> kPChunkShift;
         for (int c = 0; c < n_chunks; c++) {
-            const int p0 = start + (c << kChunkShift);
+            const int p0 = start + (c << kPChunkShift);
             if (c + 1 < n_chunks) {
-                pair_stage(&wb[(c + 1) & 1], W.pq, p0 + kChunkLen,
-                           min(kChunkLen, W.npp - (p0 + kChunkLen)), lane);
+                pair_stage(&wb[(c + 1) & 1], W.pq, p0 + kPChunkLen,
+                           min(kPChunkLen, W.npp - (p0 + kPChunkLen)), lane);
                 asm volatile("cp.async.wait_group 1;\n" ::: "memory");
             } else {
                 asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -568,7 +610,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 }
                 A = An;
             }
-            const int n_here = min(kChunkLen, W.n_pts - (c << kChunkShift));
+            const int n_here = min(kPChunkLen, W.n_pts - (c << kPChunkShift));
             // One step: point l of the chunk into q2, deposit q1 -> q2.  The
             // loop below alternates the roles of p1 and p2, so the point
             // state is never copied.
@@ -651,7 +693,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 }
             };
             if (PINGPONG) {
-                // chunks are kChunkLen (even) points long, so point l of every
+                // chunks are kPChunkLen (even) points long, so point l of every
                 // chunk lives in p1 for even l and in p2 for odd l, and the
                 // point before a chunk in p2
                 for (int l = 0; l < n_here; l += 2) {

@@ -113,6 +113,17 @@ __device__ __forceinline__ PixelCtx make_pixel(double3 P, double t0, double dt, 
     return c;
 }
 
+// v <- R v in the set's frame (FP64)
+__device__ __forceinline__ void to_frame(const Frame& F, double& x, double& y, double& z) {
+    if (F.identity) return;
+    const double a = fma(F.r[0], x, fma(F.r[1], y, F.r[2] * z));
+    const double b = fma(F.r[3], x, fma(F.r[4], y, F.r[5] * z));
+    const double c = fma(F.r[6], x, fma(F.r[7], y, F.r[8] * z));
+    x = a;
+    y = b;
+    z = c;
+}
+
 // Arrival coordinates are held relative to the current anchor's integer bin
 // B as (ki, r): (ts - t0)/dt = B + ki + r, |r| <= 1/2 normally.  B is kept
 // within +-2^29 so that B + ki never overflows 32 bits; anchors farther out

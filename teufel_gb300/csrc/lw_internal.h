@@ -24,6 +24,9 @@ constexpr int kSegLen = 1 << kSegShift;
 constexpr int kChunkShift = 5;
 constexpr int kChunkLen = 1 << kChunkShift;
 
+// float4 per pair-point of the pair kernel's interleaved data (lw_fp32_pair.cu)
+constexpr int kPairPoint = 10;
+
 // The frame the FP32 per-point vectors of a set are expressed in: v' = R v
 // (row-major r).  Its z axis is the set's mean direction of motion, so that
 // the transverse components of all directions that matter stay small and
@@ -66,7 +69,7 @@ struct DevTraj {
     int64_t n_pair_segments;
     const int64_t* pair_offsets;      // [n_pairs+1] first pair-point of each pair
     const int64_t* pair_seg_offsets;  // [n_pairs+1] first pair-segment of each pair
-    const float4* pq;                 // [pair-points][8]
+    const float4* pq;                 // [pair-points][kPairPoint]
 };
 
 // One observer handed to a kernel launch.

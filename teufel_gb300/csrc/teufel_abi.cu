@@ -444,7 +444,8 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
         (rc = dev_alloc(h, &p_aa, N)) || (rc = dev_alloc(h, &p_q0, N)) ||
         (rc = dev_alloc(h, &p_q1, N)) || (rc = dev_alloc(h, &p_q2, N)) ||
         (rc = dev_alloc(h, &p_q3, N)) || (rc = dev_alloc(h, &p_poff, n_pairs + 1)) ||
-        (rc = dev_alloc(h, &p_pseg, n_pairs + 1)) || (rc = dev_alloc(h, &p_pq, 8 * NP)))
+        (rc = dev_alloc(h, &p_pseg, n_pairs + 1)) ||
+        (rc = dev_alloc(h, &p_pq, (size_t)kPairPoint * NP)))
         return fail(rc);
     if (cudaMalloc(&h->d_status, sizeof(unsigned int)) != cudaSuccess ||
         cudaMalloc(&h->d_counters, sizeof(h->last_counters)) != cudaSuccess)
