@@ -82,16 +82,20 @@ __device__ __forceinline__ double approx_retarded_time(const double4_32a tx, con
 __device__ __forceinline__ void inwindow_steps(const double4_32a* tx, int st_lo, int st_hi,
                                                const double3 obs, const Window& w, int* first,
                                                int* last) {
-    // first point with ts > tmin in [st_lo, st_hi]
+    // first point with ts > tmin in [st_lo, st_hi]; one evaluation when the
+    // window opens before the range does
     int lo = st_lo, hi = st_hi + 1;
+    if (approx_retarded_time(tx[st_lo], obs) > w.tmin) hi = lo;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
         if (approx_retarded_time(tx[mid], obs) > w.tmin) hi = mid; else lo = mid + 1;
     }
     int i_first = lo;
-    // last point with ts < tmax in [st_lo, st_hi]
+    // last point with ts < tmax in [st_lo, st_hi]; one evaluation when the
+    // window closes after the range does
     lo = st_lo - 1;
     hi = st_hi;
+    if (approx_retarded_time(tx[st_hi], obs) < w.tmax) lo = hi;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (approx_retarded_time(tx[mid], obs) < w.tmax) lo = mid; else hi = mid - 1;

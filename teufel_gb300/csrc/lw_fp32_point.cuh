@@ -179,11 +179,12 @@ __device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, cons
     A.B = (long long)fl;
     A.Bi = (int)fl;
     A.frac = (float)(u - fl);
-    // our rounding: t, P^.x/c and their sum, G/c, the sum with Tp, the scaling
-    const float own = (float)((fabs(a.x) + fabs(pa) * ic + fabs(px.Tp) + G * ic) * px.inv_dt *
-                              4.5e-16) +
-                      (float)(fabs(u) * 4.5e-16) + 1.0e-7f;
-    A.err = own + px.refb0 + (float)(fabs(a.x) * px.inv_dt * 4.5e-16);
+    // our rounding (t, P^.x/c and their sum, G/c, the sum with Tp, the
+    // scaling: (|t| + |P^.x|/c + |Tp| + G/c)/dt + |u|, times 4.5e-16), the
+    // reference's rounding of t + R/c (|t|/dt times 4.5e-16) and of t0 and the
+    // flight time (refb0), and 1e-7 for the FP32 remainder
+    const double mag = fma(fabs(pa) + G, ic, 2.0 * fabs(a.x) + fabs(px.Tp));
+    A.err = (float)(fma(mag, px.inv_dt, fabs(u)) * 4.5e-16) + (1.0e-7f + px.refb0);
     if (u != u0) A.err = 1.0f;  // clamped: resolve the segment exactly
 }
 __device__ __forceinline__ void make_anchor(Anchor& A, const double4_32a a, const PixelCtx& px,
