@@ -119,10 +119,11 @@ cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWo
                              int variant, cudaStream_t s);
 cudaError_t launch_fp64(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int threads,
                         cudaStream_t s);
+// out += sum of the slots' partial traces over bins [e0, e1) (e1 < 0: all)
 cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* out,
-                               cudaStream_t s);
+                               cudaStream_t s, int64_t e0 = 0, int64_t e1 = -1);
 cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* out,
-                               cudaStream_t s);
+                               cudaStream_t s, int64_t e0 = 0, int64_t e1 = -1);
 cudaError_t launch_point_decisions(const DevTraj& tr, int m, double3 pos, double t0, double dt,
                                    int nt, int64_t n_points, int64_t* idx, int* flags,
                                    double* u_est, float* band, cudaStream_t s);

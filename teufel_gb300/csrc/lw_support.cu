@@ -55,8 +55,9 @@ __device__ __forceinline__ void reduce_fp32_bin(const DevWork& w, int64_t e, dou
     }
 }
 
-__global__ void reduce_fp32_kernel(DevWork w, int64_t n_bins, double* out) {
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
+// bins [e0, e1) of the observer
+__global__ void reduce_fp32_kernel(DevWork w, int64_t e0, int64_t e1, double* out) {
+    for (int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < e1;
          e += (int64_t)gridDim.x * blockDim.x)
         reduce_fp32_bin(w, e, out);
 }
@@ -76,9 +77,9 @@ __global__ void reduce_fp32_batch_kernel(const DevWork* wks, double* const* outs
     }
 }
 
-__global__ void reduce_fp64_kernel(DevWork w, int64_t n_bins, double* out) {
+__global__ void reduce_fp64_kernel(DevWork w, int64_t e0, int64_t e1, double* out) {
     const double* scr = static_cast<const double*>(w.scratch);
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_bins;
+    for (int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < e1;
          e += (int64_t)gridDim.x * blockDim.x) {
         double acc[6] = {0, 0, 0, 0, 0, 0};
         for (int s = 0; s < w.n_slots; s++) {
@@ -110,10 +111,10 @@ static unsigned reduce_blocks(int64_t n_bins) {
 }
 
 cudaError_t launch_reduce_fp32(const DevWork& w, const DevScreen& sc, double* out,
-                               cudaStream_t s) {
-    int64_t n = (int64_t)sc.np * sc.nt;
-    if (n == 0) return cudaSuccess;
-    reduce_fp32_kernel<<<reduce_blocks(n), 256, 0, s>>>(w, n, out);
+                               cudaStream_t s, int64_t e0, int64_t e1) {
+    if (e1 < 0) e1 = (int64_t)sc.np * sc.nt;
+    if (e1 <= e0) return cudaSuccess;
+    reduce_fp32_kernel<<<reduce_blocks(e1 - e0), 256, 0, s>>>(w, e0, e1, out);
     return cudaGetLastError();
 }
 
@@ -128,10 +129,10 @@ cudaError_t launch_reduce_fp32_batch(const DevWork* wks, const DevScreen* scs,
 }
 
 cudaError_t launch_reduce_fp64(const DevWork& w, const DevScreen& sc, double* out,
-                               cudaStream_t s) {
-    int64_t n = (int64_t)sc.np * sc.nt;
-    if (n == 0) return cudaSuccess;
-    reduce_fp64_kernel<<<reduce_blocks(n), 256, 0, s>>>(w, n, out);
+                               cudaStream_t s, int64_t e0, int64_t e1) {
+    if (e1 < 0) e1 = (int64_t)sc.np * sc.nt;
+    if (e1 <= e0) return cudaSuccess;
+    reduce_fp64_kernel<<<reduce_blocks(e1 - e0), 256, 0, s>>>(w, e0, e1, out);
     return cudaGetLastError();
 }
 

@@ -45,6 +45,11 @@ struct teufel_traj_set {
     std::vector<int64_t> h_seg_offsets;
     int last_slots = 0;
     bool counted = false;  // included in the live-set count of its device
+    // host-buffer calls: a copy stream that moves the trace buffer while the
+    // integration runs, and its events ([0] caller's work issued, [1] traces
+    // uploaded, [2] copies done, then one per reduced chunk)
+    cudaStream_t copy_s = nullptr;
+    std::vector<cudaEvent_t> cev;
 };
 
 namespace {
@@ -206,9 +211,20 @@ TuneKey tune_key(const teufel_traj_set* h, int np, int nt) {
                    log2_bucket(h->dev.n_points / n)};
 }
 
+// A host trace buffer behind d_out: the reduction waits for its upload
+// (uploaded, on the copy stream) and the last pass reduces in n_chunks row
+// chunks, each copied back on the copy stream as soon as it is final.
+struct HostOut {
+    double* host;
+    cudaStream_t cs;
+    cudaEvent_t uploaded;
+    const cudaEvent_t* chunk_ev;
+    int n_chunks;
+};
+
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
                int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
-               int slot_pct = 100) {
+               int slot_pct = 100, const HostOut* ho = nullptr) {
     teufel_options opt = opt_in;
     const bool fp64 = opt.precision == TEUFEL_PREC_FP64;
     if (!fp64 && opt.kernel_variant == 0) {
@@ -301,8 +317,25 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                              : launch_fp32(h->dev, sc, w, variant, s);
         if (e != cudaSuccess) return cuda_fail(e);
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 1], s));
-        e = fp64 ? launch_reduce_fp64(w, sc, d_out, s) : launch_reduce_fp32(w, sc, d_out, s);
-        if (e != cudaSuccess) return cuda_fail(e);
+        if (ho && p0 == 0) TRY_CUDA(cudaStreamWaitEvent(s, ho->uploaded, 0));
+        if (ho && p0 + per_pass >= slots_total) {
+            const int64_t n_bins = (int64_t)np * nt;
+            for (int k = 0; k < ho->n_chunks; k++) {
+                const int64_t e0 = n_bins * k / ho->n_chunks, e1 = n_bins * (k + 1) / ho->n_chunks;
+                e = fp64 ? launch_reduce_fp64(w, sc, d_out, s, e0, e1)
+                         : launch_reduce_fp32(w, sc, d_out, s, e0, e1);
+                if (e != cudaSuccess) return cuda_fail(e);
+                TRY_CUDA(cudaEventRecord(ho->chunk_ev[k], s));
+                TRY_CUDA(cudaStreamWaitEvent(ho->cs, ho->chunk_ev[k], 0));
+                if (e1 > e0)
+                    TRY_CUDA(cudaMemcpyAsync(ho->host + 6 * e0, d_out + 6 * e0,
+                                             sizeof(double) * 6 * (size_t)(e1 - e0),
+                                             cudaMemcpyDeviceToHost, ho->cs));
+            }
+        } else {
+            e = fp64 ? launch_reduce_fp64(w, sc, d_out, s) : launch_reduce_fp32(w, sc, d_out, s);
+            if (e != cudaSuccess) return cuda_fail(e);
+        }
         if (h->last_timed) {
             TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 2], s));
             h->n_ev_used += 4;
@@ -653,6 +686,8 @@ int teufel_cuda_traj_free(teufel_traj_set* traj) {
     if (traj->d_status) cudaFree(traj->d_status);
     if (traj->d_counters) cudaFree(traj->d_counters);
     for (cudaEvent_t e : traj->ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : traj->cev) cudaEventDestroy(e);
+    if (traj->copy_s) cudaStreamDestroy(traj->copy_s);
     delete traj;
     return TEUFEL_OK;
 }
@@ -689,15 +724,31 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     if ((rc = grow((void**)&h->d_out, &h->out_cap, sizeof(double) * nout, false))) return rc;
     double* d_pos = h->d_pix;
     double* d_t0 = h->d_pix + 3 * (size_t)Np;
+    // The trace buffer moves on the copy stream: up while the integration
+    // kernel runs, back chunk by chunk behind the reduction.
+    constexpr int kOutChunks = 8;
+    if (!h->copy_s) TRY_CUDA(cudaStreamCreateWithFlags(&h->copy_s, cudaStreamNonBlocking));
+    while (h->cev.size() < 3 + (size_t)kOutChunks) {
+        cudaEvent_t e;
+        TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        h->cev.push_back(e);
+    }
+    TRY_CUDA(cudaEventRecord(h->cev[0], s));
+    TRY_CUDA(cudaStreamWaitEvent(h->copy_s, h->cev[0], 0));
     TRY_CUDA(cudaMemcpyAsync(d_pos, pix_pos, sizeof(double) * 3 * Np, cudaMemcpyHostToDevice, s));
     TRY_CUDA(cudaMemcpyAsync(d_t0, pix_t0, sizeof(double) * Np, cudaMemcpyHostToDevice, s));
-    TRY_CUDA(cudaMemcpyAsync(h->d_out, out, sizeof(double) * nout, cudaMemcpyHostToDevice, s));
-    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s);
+    TRY_CUDA(cudaMemcpyAsync(h->d_out, out, sizeof(double) * nout, cudaMemcpyHostToDevice,
+                             h->copy_s));
+    TRY_CUDA(cudaEventRecord(h->cev[1], h->copy_s));
+    const HostOut ho{out, h->copy_s, h->cev[1], h->cev.data() + 3, kOutChunks};
+    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s, 100, &ho);
     if (rc) {
+        cudaStreamSynchronize(h->copy_s);
         cudaStreamSynchronize(s);
         return rc;
     }
-    TRY_CUDA(cudaMemcpyAsync(out, h->d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaEventRecord(h->cev[2], h->copy_s));
+    TRY_CUDA(cudaStreamWaitEvent(s, h->cev[2], 0));
     return finish(h, s);
 }
 
