@@ -40,7 +40,7 @@ FLOPS_PER_EXTRA_BIN = 14.0
 # DRAM bytes (read + write) per in-window (pixel, particle, step) of the pair
 # kernel, from one ncu capture of a 5000-pixel, 32-particle, 2048-sample case:
 # 2.401e9 B / 2.475e8 in-window steps
-DRAM_BYTES_PER_INWINDOW_STEP = 9.70
+DRAM_BYTES_PER_INWINDOW_STEP = 9.74
 
 
 def parse():
@@ -452,7 +452,7 @@ def run_gb300(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": DRAM_BYTES_PER_INWINDOW_STEP * inwin / max(K, 1),
-                         "traffic_note": "DRAM bytes per launch: ncu's 9.70 B per in-window "
+                         "traffic_note": "DRAM bytes per launch: ncu's 9.74 B per in-window "
                                          "step on a small case, times the in-window steps of "
                                          "one launch (an estimate)",
                          "kernel": KERNEL_NAMES.get(tuned["kernel_variant"] if tuned

@@ -85,8 +85,12 @@ def test_diffraction_screen_through_the_observer_layer(driver, fixture, tmp_path
         rtol=1e-12)
 
 
-@pytest.mark.parametrize("precision", [abi.PREC_FP32_SPLIT, abi.PREC_FP64])
-def test_diffraction_screen_with_the_device_pusher(fixture, precision):
+@pytest.mark.parametrize("precision,variant", [(abi.PREC_FP32_SPLIT, 4), (abi.PREC_FP32_SPLIT, 1),
+                                               (abi.PREC_FP32_SPLIT, 2), (abi.PREC_FP64, 0)])
+def test_diffraction_screen_with_the_device_pusher(fixture, precision, variant):
+    """Variants: 4 the pair kernel (default), 1 the warp-uniform kernel, 2 the
+    lane-divergent kernel; all use the exact arrival increment of steps that
+    pass close to the observation point."""
     fx = fixture
     with abi.TrajSet.track(fx["init"], float(fx["charge"]), float(fx["mass"]), abi.lattice(),
                            float(fx["tstep"]), int(fx["n_steps"])) as ts:
@@ -96,7 +100,7 @@ def test_diffraction_screen_with_the_device_pusher(fixture, precision):
         np.testing.assert_allclose(x[idx], fx["check_x"], rtol=1e-13, atol=1e-13)
         np.testing.assert_allclose(p[idx], fx["check_p"], rtol=1e-13)
         traces = ts.integrate_screen(fx["pos"], fx["t0"], float(fx["dt"]), int(fx["nt"]),
-                                     precision=precision)
+                                     precision=precision, variant=variant)
     energy, _ = lw.mesh_energy(fx["corner"], fx["tri"].astype(np.int64), traces,
                                float(fx["dt"]))
     check_against_reference(fx, traces, energy)
