@@ -95,3 +95,30 @@ def test_bad_tracking_arguments():
         abi.TrajSet.track(init, 1.0, 0.0, abi.lattice(), 1e-12, 10)   # zero mass
     with pytest.raises(abi.TeufelError):
         abi.TrajSet.track(init, 1.0, 1.0, abi.lattice(), -1e-12, 10)  # negative step
+
+
+@pytest.mark.parametrize("name", ["undulator", "magnet", "ecrossb"])
+def test_device_pusher_passes_the_reference_tests(name):
+    """tests/teufel.undulator.cpp, teufel.magnet.cpp and teufel.EcrossB.cpp
+    (restated in tests/pusher_cases.py) on the device pusher, which also
+    matches the host pusher: bit for bit in homogeneous fields, within 1e-12
+    in the undulator (the device's sin/cos/sinh/cosh)."""
+    from pusher_cases import CASES
+    setup, check = CASES[name]()
+    u = setup["undulator"] or {}
+    lat = abi.lattice(b_peak=u.get("b_peak", 0.0), lambda_u=u.get("lambda_u", 1.0),
+                      n_periods=u.get("n_periods", 0), origin=u.get("origin", (0.0, 0.0, 0.0)),
+                      E=setup["E"], B=setup["B"])
+    with abi.TrajSet.track(setup["init"], -1.0, 1.0, lat, setup["tstep"], setup["n_steps"]) as ts:
+        t, x, p, a = ts.download()
+    assert check(t, x, p) == []
+    hl = H.Lattice(b_peak=u.get("b_peak", 0.0), lambda_u=u.get("lambda_u", 1.0),
+                   n_periods=u.get("n_periods", 0), origin=u.get("origin", (0.0, 0.0, 0.0)),
+                   hom_e=setup["E"], hom_b=setup["B"])
+    ref = H.track(setup["init"], hl, setup["tstep"], setup["n_steps"], -1.0, 1.0)
+    assert np.array_equal(t, ref.t)
+    if name == "undulator":
+        assert rel(x, ref.x) < 1e-12 and rel(p, ref.p) < 1e-12 and rel(a, ref.a) < 1e-11
+    else:
+        for got, want in ((x, ref.x), (p, ref.p), (a, ref.a)):
+            assert np.array_equal(got, want)
