@@ -780,6 +780,40 @@ cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWo
 constexpr int kBatchMaxReg = 128;
 int pair_batch_blocks_per_sm() { return 65536 / (32 * kBatchMaxReg); }
 
+int pair_blocks_per_sm(int variant) {
+    // occupancy of the kernel of each variant, asked once
+    static int cached[4] = {-1, -1, -1, -1};
+    const int k = variant == kVariantPair160 ? 1 : variant == kVariantPair136 ? 2
+                : variant == kVariantPair144 ? 3 : 0;
+    if (cached[k] >= 0) return cached[k];
+    int n = 0;
+    cudaError_t e;
+    switch (k) {
+        case 1:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<160, true>,
+                                                              kPThreads, 0);
+            break;
+        case 2:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<136, false>,
+                                                              kPThreads, 0);
+            break;
+        case 3:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<144, true>,
+                                                              kPThreads, 0);
+            break;
+        default:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<128, false>,
+                                                              kPThreads, 0);
+            break;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cached[k] = n;
+    return n;
+}
+
 cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
                                    const BatchItem* items, int n_items, unsigned int* head,
                                    int n_blocks, cudaStream_t s) {

@@ -174,6 +174,8 @@ cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, con
                                    const BatchItem* items, int n_items, unsigned int* head,
                                    int n_blocks, cudaStream_t s);
 int pair_batch_blocks_per_sm();
+// resident one-warp blocks per SM of the pair kernel of a variant (0: unknown)
+int pair_blocks_per_sm(int variant);
 constexpr int kPairTile = 32;  // pixels per tile of the pair kernel
 cudaError_t launch_reduce_fp32_batch(const DevWork* wks, const DevScreen* scs,
                                      double* const* outs, const int64_t* bin_prefix, int n_obs,

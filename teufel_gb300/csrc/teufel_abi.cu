@@ -222,6 +222,33 @@ struct HostOut {
     int n_chunks;
 };
 
+// The slot count near `slots` that best fills the last wave of the pair
+// kernel's grid (pixel tiles x slots one-warp blocks, equal work each): the
+// estimated time ceil(blocks / resident) / slots is minimised over
+// [3/4, 3/2] x slots, taking the smallest count within 2% of the best, since
+// every slot adds a partial trace to reduce.
+int64_t fill_waves(const teufel_traj_set* h, int np, int variant, int64_t slots) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
+        cudaGetLastError();
+        return slots;
+    }
+    const int64_t resident = (int64_t)pair_blocks_per_sm(variant) * sms;
+    const int64_t tiles = (np + kPairTile - 1) / kPairTile;
+    if (resident <= 0 || tiles <= 0) return slots;
+    const int64_t lo = std::max<int64_t>(1, (3 * slots + 3) / 4);
+    const int64_t hi = std::max<int64_t>(lo, std::min<int64_t>(3 * slots / 2,
+                                                               h->dev.n_pair_segments));
+    auto cost = [&](int64_t s) {
+        return (double)((tiles * s + resident - 1) / resident) / (double)s;
+    };
+    double best = cost(slots);
+    for (int64_t s = lo; s <= hi; s++) best = std::min(best, cost(s));
+    for (int64_t s = lo; s <= hi; s++)
+        if (cost(s) <= 1.02 * best) return s;
+    return slots;
+}
+
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
                int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
                int slot_pct = 100, const HostOut* ho = nullptr) {
@@ -260,6 +287,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     if (!fp64 && opt.n_slots <= 0)
         slots_total = std::max<int64_t>(slots_total,
                                         (units + max_units_per_slot - 1) / max_units_per_slot);
+    if (pairs && opt.n_slots <= 0) slots_total = fill_waves(h, np, variant, slots_total);
     slots_total = std::min<int64_t>(slots_total, std::max<int64_t>(G, 1));
     cudaMemPool_t pool = scratch_pool(h->device);
     if (!pool) return TEUFEL_ERR_CUDA;
