@@ -7,52 +7,63 @@
 
 namespace teufel {
 
-// out[p][k][c] += sum over slots (in slot order, FP64) of the partial
-// traces; the partial slots are cleared for the next call.  The FP32 path
-// stores c*B, so the B components are divided by c here.
 // out[e] += the sum over slots of the FP32 partial traces of bin e (B from
-// cB), and the partial traces cleared for the next use.
+// cB), and the partial traces cleared for the next use.  The slots are summed
+// in slot order in FP32 with Kahan compensation (on the FP32 pipe: FP64 runs at
+// 1/64 of its rate here), and each component enters FP64 once, as its sum
+// plus compensation; the error of the sum is a few FP32 ulps of the smallest
+// partial, far below the partials' own rounding.
 __device__ __forceinline__ void reduce_fp32_bin(const DevWork& w, int64_t e, double* out) {
     const float* scr = static_cast<const float*>(w.scratch);
-    {
-        double acc[6] = {0, 0, 0, 0, 0, 0};
-        // all loads first (independent, so they overlap), then the clears
-        for (int s = 0; s < w.n_slots; s++) {
-            const float2* p = (const float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
-            const float2 a = __ldcs(p), b = __ldcs(p + 1), c = __ldcs(p + 2);
-            acc[0] += (double)a.x;
-            acc[1] += (double)a.y;
-            acc[2] += (double)b.x;
-            acc[3] += (double)b.y;
-            acc[4] += (double)c.x;
-            acc[5] += (double)c.y;
-        }
-        const float2 z = make_float2(0.0f, 0.0f);
-        for (int s = 0; s < w.n_slots; s++) {
-            float2* p = (float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
-            __stcs(p, z);
-            __stcs(p + 1, z);
-            __stcs(p + 2, z);
-        }
-        if (!w.frame.identity) {
-            // from the set's frame back to the observer's: v = R^T v'
-            const double* r = w.frame.r;
-#pragma unroll
-            for (int k = 0; k < 6; k += 3) {
-                const double a = acc[k], b = acc[k + 1], c = acc[k + 2];
-                acc[k] = fma(r[0], a, fma(r[3], b, r[6] * c));
-                acc[k + 1] = fma(r[1], a, fma(r[4], b, r[7] * c));
-                acc[k + 2] = fma(r[2], a, fma(r[5], b, r[8] * c));
-            }
-        }
-        double* o = out + e * 6;
-        o[0] += acc[0];
-        o[1] += acc[1];
-        o[2] += acc[2];
-        o[3] += acc[3] / kC;
-        o[4] += acc[4] / kC;
-        o[5] += acc[5] / kC;
+    float sum[6] = {0, 0, 0, 0, 0, 0}, cmp[6] = {0, 0, 0, 0, 0, 0};
+    auto kahan = [&](int k, float x) {
+        const float y = x - cmp[k];
+        const float t = sum[k] + y;
+        cmp[k] = (t - sum[k]) - y;
+        sum[k] = t;
+    };
+    // all loads first (independent, so they overlap), then the clears
+    for (int s = 0; s < w.n_slots; s++) {
+        const float2* p = (const float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
+        const float2 a = __ldcs(p), b = __ldcs(p + 1), c = __ldcs(p + 2);
+        kahan(0, a.x);
+        kahan(1, a.y);
+        kahan(2, b.x);
+        kahan(3, b.y);
+        kahan(4, c.x);
+        kahan(5, c.y);
     }
+    const float2 z = make_float2(0.0f, 0.0f);
+    for (int s = 0; s < w.n_slots; s++) {
+        float2* p = (float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
+        __stcs(p, z);
+        __stcs(p + 1, z);
+        __stcs(p + 2, z);
+    }
+    double acc[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) acc[k] = (double)sum[k] - (double)cmp[k];
+    if (!w.frame.identity) {
+        // from the set's frame back to the observer's: v = R^T v'
+        const double* r = w.frame.r;
+#pragma unroll
+        for (int k = 0; k < 6; k += 3) {
+            const double a = acc[k], b = acc[k + 1], c = acc[k + 2];
+            acc[k] = fma(r[0], a, fma(r[3], b, r[6] * c));
+            acc[k + 1] = fma(r[1], a, fma(r[4], b, r[7] * c));
+            acc[k + 2] = fma(r[2], a, fma(r[5], b, r[8] * c));
+        }
+    }
+    // B = (cB) / c, as a product with the rounded 1/c (within an ulp of the
+    // quotient; an FP64 division costs ten times as much)
+    constexpr double kInvC = 1.0 / kC;
+    double* o = out + e * 6;
+    o[0] += acc[0];
+    o[1] += acc[1];
+    o[2] += acc[2];
+    o[3] += acc[3] * kInvC;
+    o[4] += acc[4] * kInvC;
+    o[5] += acc[5] * kInvC;
 }
 
 // bins [e0, e1) of the observer
