@@ -44,30 +44,39 @@ namespace teufel {
 // ---------------------------------------------------------------------------
 // Per-point preparation (pixel independent), run once after upload
 // ---------------------------------------------------------------------------
+// One warp per particle: the lanes test the steps in parallel.
 __global__ void prep_particles_kernel(DevTraj tr, double4_32a* vhat) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.x;
     if (m >= tr.n_particles) return;
-    int64_t o = tr.offsets[m], n = tr.offsets[m + 1] - o;
+    const int64_t o = tr.offsets[m], n = tr.offsets[m + 1] - o;
+    // Arrival times increase along the trajectory for every observer when
+    // time increases and every chord is slower than light (triangle
+    // inequality); the range bisection relies on it.
+    bool mono = true;
+    for (int64_t i = o + threadIdx.x; i + 1 < o + n; i += 32) {
+        const double4_32a p = tr.tx[i], q = tr.tx[i + 1];
+        const double ddt = q.x - p.x;
+        const double ex = q.y - p.y, ey = q.z - p.z, ez = q.w - p.w;
+        const double cd = kC * ddt;
+        mono = mono && (ddt > 0.0) && (ex * ex + ey * ey + ez * ez < 0.999999 * cd * cd);
+    }
+    mono = __all_sync(0xffffffffu, mono);
+    if (threadIdx.x != 0) return;
     double4_32a v = make_double4_32a(0.0, 0.0, 1.0, 0.0);
     if (n >= 2) {
-        double4_32a a = tr.tx[o], b = tr.tx[o + n - 1];
-        double dx = b.y - a.y, dy = b.z - a.z, dz = b.w - a.w;
-        double L = sqrt(dx * dx + dy * dy + dz * dz);
+        const double4_32a a = tr.tx[o], b = tr.tx[o + n - 1];
+        const double dx = b.y - a.y, dy = b.z - a.z, dz = b.w - a.w;
+        const double L = sqrt(dx * dx + dy * dy + dz * dz);
         if (L > 0.0) v = make_double4_32a(dx / L, dy / L, dz / L, 0.0);
-        // Arrival times increase along the trajectory for every observer when
-        // time increases and every chord is slower than light (triangle
-        // inequality); the range bisection relies on it.
-        bool mono = true;
-        for (int64_t i = o; i + 1 < o + n && mono; i++) {
-            double4_32a p = tr.tx[i], q = tr.tx[i + 1];
-            double ddt = q.x - p.x;
-            double ex = q.y - p.y, ey = q.z - p.z, ez = q.w - p.w;
-            double cd = kC * ddt;
-            mono = (ddt > 0.0) && (ex * ex + ey * ey + ez * ez < 0.999999 * cd * cd);
-        }
         v.w = mono ? 1.0 : 0.0;
     }
     vhat[m] = v;
+}
+
+cudaError_t launch_prep_particles(const DevTraj& tr, cudaStream_t s) {
+    if (tr.n_particles > 0)
+        prep_particles_kernel<<<tr.n_particles, 32, 0, s>>>(tr, const_cast<double4_32a*>(tr.vhat));
+    return cudaGetLastError();
 }
 
 __global__ void prep_points_kernel(DevTraj tr, float4* q0, float4* q1, float4* q2, float4* q3) {
@@ -120,14 +129,6 @@ __global__ void prep_points_kernel(DevTraj tr, float4* q0, float4* q1, float4* q
     to_frame(tr.frame, ax, ay, az);
     q2[i] = make_float4((float)(ax * sa), (float)(ay * sa), (float)(az * sa),
                         (float)(scale / (gamma * gamma)));
-}
-
-cudaError_t launch_prep_particles(const DevTraj& tr, cudaStream_t s) {
-    if (tr.n_particles > 0) {
-        prep_particles_kernel<<<(tr.n_particles + 127) / 128, 128, 0, s>>>(
-            tr, const_cast<double4_32a*>(tr.vhat));
-    }
-    return cudaGetLastError();
 }
 
 // After the set's frame is known (from the particles' directions).
