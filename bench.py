@@ -39,7 +39,7 @@ FLOPS_PER_STEP = 110.0
 FLOPS_PER_EXTRA_BIN = 14.0
 # DRAM bytes (read + write) per in-window (pixel, particle, step) of the pair
 # kernel, from one ncu capture of a 5000-pixel, 32-particle, 2048-sample case:
-# 2.401e9 B / 2.475e8 in-window steps
+# 2.408e9 B / 2.474e8 in-window steps
 DRAM_BYTES_PER_INWINDOW_STEP = 9.74
 
 
@@ -64,6 +64,8 @@ def parse():
                     help="skip the batched-observer measurement")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the FP32-vs-FP64 comparison on the other workloads")
     return ap.parse_args()
 
 
@@ -196,6 +198,40 @@ def batch_measure(dev, reps=2, scale=64):
             "workload": f"16 seeded screens of the batched uneven-observer configuration "
                         f"(meshes 16^2..128^2, 512..8192 samples, 2e3..2e4 steps), each with "
                         f"its particle draw / {scale} (min 4)"}
+
+
+def other_workloads():
+    """FP32-split against FP64-GPU throughput and accuracy on the other
+    workloads (untimed by the driver; each path runs once after a warm-up):
+    the single electron on the 21x21 screen in full, a 128-particle draw of
+    the 1e4-particle bunch on its 64x64 screen, and a 64-particle draw of the
+    gamma = 2000 bunch (multi-bin steps) on every 4th pixel of its 100x100
+    screen."""
+    from teufel_gb300 import abi, harness as H
+    cases = [("single_electron_21x21_2048x5fs", H.config1(), None),
+             ("bunch_1e4_100pC_64x64_2048x5fs_128_particles", H.config2(count=128), None),
+             ("gamma2000_bunch_1e3_100x100_8192x1as_64_particles_every_4th_pixel",
+              H.config5(count=64), 4)]
+    out = {}
+    for name, w, every in cases:
+        if every:
+            w = w.pixel_subset(np.arange(0, w.n_pix, every))
+        evals = w.n_pix * int(np.sum(np.maximum(w.traj.n_points.astype(np.int64) - 1, 0)))
+        res = {}
+        with abi.TrajSet(w.traj) as ts:
+            for prec, key in ((abi.PREC_FP64, "fp64"), (abi.PREC_FP32_SPLIT, "fp32")):
+                ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
+                tt = time.perf_counter()
+                r = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
+                res[key] = (r, time.perf_counter() - tt)
+        ref = res["fp64"][0]
+        out[name] = {"evals": evals, "pixels": w.n_pix, "particles": w.traj.n_particles,
+                     "fp32_split_evals_per_s": evals / res["fp32"][1],
+                     "fp64_gpu_evals_per_s": evals / res["fp64"][1],
+                     "speedup_fp32_split_over_fp64": res["fp64"][1] / res["fp32"][1],
+                     "rel_l2_fp32_split_vs_fp64":
+                         float(np.linalg.norm(res["fp32"][0] - ref) / np.linalg.norm(ref))}
+    return out
 
 
 def shard(n, rank, world):
@@ -421,6 +457,10 @@ def run_gb300(args):
         torch.cuda.empty_cache()
         batch = batch_measure(dev)
 
+    others = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        others = other_workloads()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -464,6 +504,7 @@ def run_gb300(args):
                          "algorithmic_flops": flops, "kernel_ms": kernel_ms,
                          "reduce_ms": reduce_ms, "fp64_probe_tflops": peak64},
             "autotune": tuned,
+            "other_workloads": others,
             "batched_observers": batch,
             "gpu_launches": launches,
             "clocks": clk,
