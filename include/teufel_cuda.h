@@ -145,7 +145,11 @@ int64_t teufel_cuda_traj_points(const teufel_traj_set *traj);
  * ScreenObserver<Beam>::integrate (src/screen.cpp:113-146): pixel i observes
  * at pix_pos[i] with trace t0 = pix_t0[i], step dt, Nt samples; the result is
  * added into out[Np][Nt][6] (host memory).  Nt < 2 or an empty particle set
- * leaves out unchanged, as the reference does (src/particle.cpp:778-783). */
+ * leaves out unchanged, as the reference does (src/particle.cpp:778-783).
+ * Synchronous at return.  The work runs on s; out travels on a stream of the
+ * set's own, ordered after the work already on s (up during the integration,
+ * back in chunks behind the reduction), so pinned memory overlaps the copies
+ * with the computation. */
 int teufel_cuda_integrate_screen(const teufel_traj_set *traj, const double *pix_pos,
                                  const double *pix_t0, double dt, int Nt, int Np, double *out,
                                  teufel_stream_t s);
