@@ -38,9 +38,10 @@ UNIT = "evals/s"
 FLOPS_PER_STEP = 110.0
 FLOPS_PER_EXTRA_BIN = 14.0
 # DRAM bytes (read + write) per in-window (pixel, particle, step) of the pair
-# kernel, from one ncu capture of a 5000-pixel, 32-particle, 2048-sample case:
-# 2.408e9 B / 2.474e8 in-window steps
-DRAM_BYTES_PER_INWINDOW_STEP = 9.74
+# kernel, from a one-pass ncu capture of one full-size bench launch (1024
+# particles, 40000 pixels, 4096 samples, 9 slots): 1.426e12 B / 9.93e10
+# in-window steps
+DRAM_BYTES_PER_INWINDOW_STEP = 14.36
 
 
 def parse():
@@ -492,9 +493,10 @@ def run_gb300(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": DRAM_BYTES_PER_INWINDOW_STEP * inwin / max(K, 1),
-                         "traffic_note": "DRAM bytes per launch: ncu's 9.74 B per in-window "
-                                         "step on a small case, times the in-window steps of "
-                                         "one launch (an estimate)",
+                         "traffic_note": "DRAM bytes per launch: 14.36 B per in-window "
+                                         "step (dram__bytes_read.sum + write.sum of one "
+                                         "full-size launch, one ncu pass) times the in-window "
+                                         "steps of one launch",
                          "kernel": KERNEL_NAMES.get(tuned["kernel_variant"] if tuned
                                                     else args.variant, "?"),
                          "peak_source": "the larger of the FFMA and packed-FFMA2 throughput "
