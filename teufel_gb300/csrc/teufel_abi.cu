@@ -222,6 +222,34 @@ struct HostOut {
     int n_chunks;
 };
 
+// Bounds of the slots in work units (segments).  Blocks are dispatched slot by
+// slot, so with equal slots the last wave drains unevenly; geometric sizes
+// (first slot largest, last ~6% of it) put the shortest blocks at the end.
+// Equal slots where the geometric first slot would hold more than max_units
+// units (particles or pairs), the FP32 accumulation limit.
+std::vector<int64_t> slot_bounds(int64_t G, int64_t slots, int64_t units, int64_t max_units,
+                                 bool geometric) {
+    std::vector<int64_t> b(slots + 1);
+    for (int64_t k = 0; k <= slots; k++) b[k] = G * k / slots;
+    if (!geometric || slots < 2 || G < 4 * slots) return b;
+    const double r = std::pow(0.06, 1.0 / (double)(slots - 1));
+    const double total = (1.0 - std::pow(r, (double)slots)) / (1.0 - r);
+    std::vector<int64_t> g(slots + 1);
+    g[0] = 0;
+    double acc = 0.0;
+    for (int64_t k = 1; k <= slots; k++) {
+        acc += std::pow(r, (double)(k - 1));
+        g[k] = std::min<int64_t>(G, (int64_t)std::llround(G * acc / total));
+        g[k] = std::max<int64_t>(g[k], g[k - 1] + 1);
+    }
+    g[slots] = G;
+    if (g[slots - 1] >= G) return b;
+    // the first slot's units, at the set's average segments per unit
+    const double per_unit = (double)G / (double)std::max<int64_t>(units, 1);
+    if ((double)g[1] / per_unit + 1.0 > (double)max_units) return b;
+    return g;
+}
+
 // The slot count near `slots` that best fills the last wave of the pair
 // kernel's grid (pixel tiles x slots one-warp blocks, equal work each): the
 // estimated time ceil(blocks / resident) / slots is minimised over
@@ -306,8 +334,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     } release{scratch, s};
     TRY_CUDA(cudaMemsetAsync(scratch, 0, scratch_bytes, s));
     h->last_slots = (int)slots_total;
-    std::vector<int64_t> bounds(slots_total + 1);
-    for (int64_t k = 0; k <= slots_total; k++) bounds[k] = G * k / slots_total;
+    std::vector<int64_t> bounds = slot_bounds(G, slots_total, units, max_units_per_slot, !fp64);
     if (h->slot_cap < slots_total + 1) {
         if (h->slot_seg) cudaFree(h->slot_seg);
         h->slot_seg = nullptr;
