@@ -203,7 +203,8 @@ def batch_measure(dev, reps=2, scale=64):
 
 def other_workloads():
     """FP32-split against FP64-GPU throughput and accuracy on the other
-    workloads (untimed by the driver; each path runs once after a warm-up):
+    workloads (untimed by the driver; FP64 once and FP32 best of three, after a
+    warm-up call each):
     the single electron on the 21x21 screen in full, a 128-particle draw of
     the 1e4-particle bunch on its 64x64 screen, and a 64-particle draw of the
     gamma = 2000 bunch (multi-bin steps) on every 4th pixel of its 100x100
@@ -220,11 +221,17 @@ def other_workloads():
         evals = w.n_pix * int(np.sum(np.maximum(w.traj.n_points.astype(np.int64) - 1, 0)))
         res = {}
         with abi.TrajSet(w.traj) as ts:
-            for prec, key in ((abi.PREC_FP64, "fp64"), (abi.PREC_FP32_SPLIT, "fp32")):
+            # after a warm-up call: the FP64 path once (seconds), the FP32 path
+            # best of three (tens of milliseconds, so single runs are noisy)
+            for prec, key, reps in ((abi.PREC_FP64, "fp64", 1), (abi.PREC_FP32_SPLIT, "fp32", 3)):
                 ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
-                tt = time.perf_counter()
-                r = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
-                res[key] = (r, time.perf_counter() - tt)
+                best = None
+                for _ in range(reps):
+                    tt = time.perf_counter()
+                    r = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
+                    el = time.perf_counter() - tt
+                    best = el if best is None else min(best, el)
+                res[key] = (r, best)
         ref = res["fp64"][0]
         out[name] = {"evals": evals, "pixels": w.n_pix, "particles": w.traj.n_particles,
                      "fp32_split_evals_per_s": evals / res["fp32"][1],

@@ -223,10 +223,10 @@ struct HostOut {
 };
 
 // Bounds of the slots in work units (segments).  Blocks are dispatched slot by
-// slot, so with equal slots the last wave drains unevenly; geometric sizes
-// (first slot largest, last ~6% of it) put the shortest blocks at the end.
-// Equal slots where the geometric first slot would hold more than max_units
-// units (particles or pairs), the FP32 accumulation limit.
+// slot, so with equal slots the last of several waves drains unevenly;
+// geometric sizes (first slot largest, last ~6% of it) put the shortest blocks
+// at the end.  Equal slots where the geometric first slot would hold more
+// than max_units units (particles or pairs), the FP32 accumulation limit.
 std::vector<int64_t> slot_bounds(int64_t G, int64_t slots, int64_t units, int64_t max_units,
                                  bool geometric) {
     std::vector<int64_t> b(slots + 1);
@@ -255,13 +255,19 @@ std::vector<int64_t> slot_bounds(int64_t G, int64_t slots, int64_t units, int64_
 // estimated time ceil(blocks / resident) / slots is minimised over
 // [3/4, 3/2] x slots, taking the smallest count within 2% of the best, since
 // every slot adds a partial trace to reduce.
-int64_t fill_waves(const teufel_traj_set* h, int np, int variant, int64_t slots) {
+// one-warp blocks of the pair kernel of `variant` resident on the device
+// (0: unknown)
+int64_t resident_pair_blocks(const teufel_traj_set* h, int variant) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
         cudaGetLastError();
-        return slots;
+        return 0;
     }
-    const int64_t resident = (int64_t)pair_blocks_per_sm(variant) * sms;
+    return (int64_t)pair_blocks_per_sm(variant) * sms;
+}
+
+int64_t fill_waves(const teufel_traj_set* h, int np, int variant, int64_t slots) {
+    const int64_t resident = resident_pair_blocks(h, variant);
     const int64_t tiles = (np + kPairTile - 1) / kPairTile;
     if (resident <= 0 || tiles <= 0) return slots;
     const int64_t lo = std::max<int64_t>(1, (3 * slots + 3) / 4);
@@ -334,7 +340,16 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     } release{scratch, s};
     TRY_CUDA(cudaMemsetAsync(scratch, 0, scratch_bytes, s));
     h->last_slots = (int)slots_total;
-    std::vector<int64_t> bounds = slot_bounds(G, slots_total, units, max_units_per_slot, !fp64);
+    // geometric slot sizes for the pair kernel's grids of three waves or more
+    // (below that the longest blocks set the time, and equal slots are best)
+    bool geometric = false;
+    if (pairs) {
+        const int64_t resident = resident_pair_blocks(h, variant);
+        const int64_t tiles = (np + kPairTile - 1) / kPairTile;
+        geometric = resident > 0 && tiles * slots_total >= 3 * resident;
+    }
+    std::vector<int64_t> bounds =
+        slot_bounds(G, slots_total, units, max_units_per_slot, geometric);
     if (h->slot_cap < slots_total + 1) {
         if (h->slot_seg) cudaFree(h->slot_seg);
         h->slot_seg = nullptr;
