@@ -39,9 +39,9 @@ FLOPS_PER_STEP = 110.0
 FLOPS_PER_EXTRA_BIN = 14.0
 # DRAM bytes (read + write) per in-window (pixel, particle, step) of the pair
 # kernel, from a one-pass ncu capture of one full-size bench launch (1024
-# particles, 40000 pixels, 4096 samples, 9 slots): 1.426e12 B / 9.93e10
+# particles, 40000 pixels, 4096 samples, 9 slots): 1.436e12 B / 9.93e10
 # in-window steps
-DRAM_BYTES_PER_INWINDOW_STEP = 14.36
+DRAM_BYTES_PER_INWINDOW_STEP = 14.47
 
 
 def parse():
@@ -500,7 +500,7 @@ def run_gb300(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": DRAM_BYTES_PER_INWINDOW_STEP * inwin / max(K, 1),
-                         "traffic_note": "DRAM bytes per launch: 14.36 B per in-window "
+                         "traffic_note": "DRAM bytes per launch: 14.47 B per in-window "
                                          "step (dram__bytes_read.sum + write.sum of one "
                                          "full-size launch, one ncu pass) times the in-window "
                                          "steps of one launch",
