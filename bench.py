@@ -153,7 +153,8 @@ def make_batches(n_batches, batch, nthreads=0):
 KERNEL_NAMES = {0: "lw_fp32_pair_kernel<128>", 1: "lw_fp32_warp_kernel<2>",
                 2: "lw_fp32_lanes_kernel", 3: "lw_fp32_warp_kernel<3>",
                 4: "lw_fp32_pair_kernel<128>", 5: "lw_fp32_pair_kernel<160>",
-                6: "lw_fp32_pair_kernel<136>", 7: "lw_fp32_pair_kernel<144>"}
+                6: "lw_fp32_pair_kernel<136>", 7: "lw_fp32_pair_kernel<144>",
+                8: "lw_fp32_pair_kernel<128, multi-bin>"}
 
 
 def batch_measure(dev, reps=2, scale=64):
@@ -204,7 +205,8 @@ def batch_measure(dev, reps=2, scale=64):
 def other_workloads():
     """FP32-split against FP64-GPU throughput and accuracy on the other
     workloads (untimed by the driver; FP64 once and FP32 best of three, after a
-    warm-up call each):
+    warm-up call each; the FP32 path tuned for the workload first, as
+    teufel_cuda_autotune does for any caller):
     the single electron on the 21x21 screen in full, a 128-particle draw of
     the 1e4-particle bunch on its 64x64 screen, and a 64-particle draw of the
     gamma = 2000 bunch (multi-bin steps) on every 4th pixel of its 100x100
@@ -221,6 +223,7 @@ def other_workloads():
         evals = w.n_pix * int(np.sum(np.maximum(w.traj.n_points.astype(np.int64) - 1, 0)))
         res = {}
         with abi.TrajSet(w.traj) as ts:
+            tv, _, _ = ts.autotune(w.pix_pos, w.pix_t0, w.dt, w.nots)
             # after a warm-up call: the FP64 path once (seconds), the FP32 path
             # best of three (tens of milliseconds, so single runs are noisy)
             for prec, key, reps in ((abi.PREC_FP64, "fp64", 1), (abi.PREC_FP32_SPLIT, "fp32", 3)):
@@ -234,6 +237,7 @@ def other_workloads():
                 res[key] = (r, best)
         ref = res["fp64"][0]
         out[name] = {"evals": evals, "pixels": w.n_pix, "particles": w.traj.n_particles,
+                     "fp32_kernel": KERNEL_NAMES.get(tv, "?"),
                      "fp32_split_evals_per_s": evals / res["fp32"][1],
                      "fp64_gpu_evals_per_s": evals / res["fp64"][1],
                      "speedup_fp32_split_over_fp64": res["fp64"][1] / res["fp32"][1],

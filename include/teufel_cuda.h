@@ -68,7 +68,9 @@ typedef struct teufel_options {
                              steps, 2 = per-pixel steps, 3 = warp-uniform steps
                              with registers for 3 blocks of 256 per SM,
                              4/5/6/7 = warp-uniform steps, two particles per
-                             thread, 16/12/15/14 resident warps per SM        */
+                             thread, 16/12/15/14 resident warps per SM,
+                             8 = as 4, with packed deposits of steps that
+                             span several bins (short bins)                  */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
 } teufel_options;
@@ -183,7 +185,8 @@ int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int
 
 /* No counterpart in the reference.  Tunes the FP32 split-precision path for
  * one observer shape: times the kernel variants (warp-uniform; two particles
- * per thread at 12 to 16 resident warps per SM) at the automatic slot count,
+ * per thread at 12 to 16 resident warps per SM, and at 16 with packed
+ * multi-bin deposits) at the automatic slot count,
  * then the fastest at half and twice as many slots, on these very inputs,
  * writing the trial traces to a scratch buffer (out-free: nothing is added
  * anywhere).  *best receives *opt with kernel_variant and n_slots set to the
@@ -191,7 +194,7 @@ int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int
  * the shape class -- the log2 sizes of Np, Nt, the particle count and the
  * points per particle -- so later calls with kernel_variant = 0 on a similar
  * shape use it.  opt->device_pointers says where pix_pos/pix_t0 live.
- * Synchronous; runs the integration about nine times. */
+ * Synchronous; runs the integration about ten times. */
 int teufel_cuda_autotune(const teufel_traj_set *traj, const double *pix_pos,
                          const double *pix_t0, double dt, int Nt, int Np,
                          const teufel_options *opt, teufel_options *best, double *best_ms);

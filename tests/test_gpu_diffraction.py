@@ -85,11 +85,13 @@ def test_diffraction_screen_through_the_observer_layer(driver, fixture, tmp_path
         rtol=1e-12)
 
 
-@pytest.mark.parametrize("precision,variant", [(abi.PREC_FP32_SPLIT, 4), (abi.PREC_FP32_SPLIT, 1),
-                                               (abi.PREC_FP32_SPLIT, 2), (abi.PREC_FP64, 0)])
+@pytest.mark.parametrize("precision,variant", [(abi.PREC_FP32_SPLIT, 4), (abi.PREC_FP32_SPLIT, 8),
+                                               (abi.PREC_FP32_SPLIT, 1), (abi.PREC_FP32_SPLIT, 2),
+                                               (abi.PREC_FP64, 0)])
 def test_diffraction_screen_with_the_device_pusher(fixture, precision, variant):
-    """Variants: 4 the pair kernel (default), 1 the warp-uniform kernel, 2 the
-    lane-divergent kernel; all use the exact arrival increment of steps that
+    """Variants: 4 the pair kernel (default), 8 the pair kernel with packed
+    multi-bin deposits, 1 the warp-uniform kernel, 2 the lane-divergent
+    kernel; all use the exact arrival increment of steps that
     pass close to the observation point."""
     fx = fixture
     with abi.TrajSet.track(fx["init"], float(fx["charge"]), float(fx["mass"]), abi.lattice(),

@@ -72,7 +72,7 @@ def test_config1_fp64_matches_oracle(c1, c1_oracle):
     assert inwin > 0
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4])
+@pytest.mark.parametrize("variant", [1, 2, 4, 8])
 def test_config1_fp32_matches_oracle(c1, c1_oracle, variant):
     with abi.TrajSet(c1.traj) as ts:
         g = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots, variant=variant)
@@ -173,7 +173,7 @@ def test_error_bound_holds(name, cfg, count, pix_step):
     print(f"{name}: largest |estimate - reference| / band = {worst:.3f} over {n_near} points")
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4])
+@pytest.mark.parametrize("variant", [1, 2, 4, 8])
 @pytest.mark.parametrize("name,cfg,count,pix_step", [
     ("config2", H.config2, 48, 37),
     ("config4", H.config4, 6, 613),
@@ -233,7 +233,7 @@ def _truncated(traj, lengths):
                           np.array(ms))
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4])
+@pytest.mark.parametrize("variant", [1, 2, 4, 8])
 def test_uneven_particle_set(variant):
     """An odd number of particles of unequal lengths, one with a single point
     and one with none: the pair kernel pads the shorter particle of a pair
@@ -314,7 +314,7 @@ def _rotated(w, R):
     return tr2, w.pix_pos @ R.T
 
 
-@pytest.mark.parametrize("variant", [1, 4])
+@pytest.mark.parametrize("variant", [1, 4, 8])
 @pytest.mark.parametrize("name,cfg,count,pix_step", [
     ("config2", H.config2, 24, 37),
     ("config4", H.config4, 6, 613),

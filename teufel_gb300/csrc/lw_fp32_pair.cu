@@ -384,6 +384,60 @@ struct PairSink {
         for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, fma(f2v[c], b2, f1[c] * a2));
         n_add += (unsigned)fa + (unsigned)fb + (unsigned)sa + (unsigned)sb;
     }
+    // Regular steps of both particles that may span several bins: ka/kb the
+    // first bin, spa/spb >= 0 the bins spanned beyond it (0 for a particle
+    // that does not deposit).  The first bin receives f1 a1 + f2 b1 and closes
+    // when the step spans; each full bin k1 + j, 0 < j < span, receives
+    // f1 w1(j) + f2 w2(j) with w1(j) = (u2 - j) rd, w2(j) = (j - u1) rd in bin
+    // units from k1 (u1 = r1, u2 = span + r2); the last bin opens with
+    // f1 a2 + f2 b2.
+    __device__ __forceinline__ void add_multi(bool fa, bool fb, int ka, int kb, int spa, int spb,
+                                              const F2* f1, const F2* f2v, F2 a1, F2 b1, F2 a2,
+                                              F2 b2, F2 u1, F2 u2, F2 rd) {
+        const bool na = fa && ka != open_a, nb = fb && kb != open_b;
+        if (na || nb) {
+            if (na) {
+                flush<0>();
+                open_a = ka;
+#pragma unroll
+                for (int c = 0; c < 6; c++) acc[c].v.x = 0.0f;
+            }
+            if (nb) {
+                flush<1>();
+                open_b = kb;
+#pragma unroll
+                for (int c = 0; c < 6; c++) acc[c].v.y = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[c] = fma(f2v[c], b1, fma(f1[c], a1, acc[c]));
+        const bool sa = spa > 0, sb = spb > 0;
+        reduce_if<0>(sa, ka);
+        reduce_if<1>(sb, kb);
+        // full bins, in bin order per particle
+        const int nfull = max(spa, spb) - 1;
+        for (int j = 1; j <= nfull; j++) {
+            const F2 jj = f2((float)j, (float)j);
+            const F2 w1 = (u2 - jj) * rd, w2 = (jj - u1) * rd;
+            F2 g[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) g[c] = fma(f2v[c], w2, f1[c] * w1);
+            const bool pa = j < spa, pb = j < spb;
+            float* qa = row + (int64_t)(ka + j) * 6;
+            float* qb = row + (int64_t)(kb + j) * 6;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                red_add2_if(pa, qa + 2 * c, g[2 * c].v.x, g[2 * c + 1].v.x);
+                red_add2_if(pb, qb + 2 * c, g[2 * c].v.y, g[2 * c + 1].v.y);
+            }
+        }
+        open_a = sa ? ka + spa : open_a;
+        open_b = sb ? kb + spb : open_b;
+        const F2 keep = f2(sa ? 0.0f : 1.0f, sb ? 0.0f : 1.0f);
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, fma(f2v[c], b2, f1[c] * a2));
+        n_add += (unsigned)fa + (unsigned)fb + (unsigned)spa + (unsigned)spb;
+    }
     template <int W>
     __device__ __forceinline__ void reduce_if(bool p, int k) {
         float* q = row + (int64_t)k * 6;
@@ -423,6 +477,40 @@ __device__ __forceinline__ void deposit_fast2(const PointState2& p1, const Point
     const F2 a1 = (f2(2.0f, 2.0f) - lam) * hw1, b1 = lam * hw1;
     const F2 a2 = (one - lam) * hw2, b2 = (one + lam) * hw2;
     sink.add_fast(fa, fb, Ba + p1.ka, Bb + p1.kb, sa, sb, p1.f, p2.f, a1, b1, a2, b2);
+}
+
+// Regular steps that span several bins (deposit_step32's first partial, full
+// and last partial bins, for both particles at once).  A step that does not
+// span (sp = 0) deposits its single-bin weight dts (f1 + f2)/2; a particle that
+// does not deposit gets zero weights and no span.
+constexpr int kMaxSpan = 16;  // bins a step of this path may span beyond its first
+
+__device__ __forceinline__ void multi_weights(bool f, int sp, float r1, float r2, float& a1,
+                                              float& b1, float& a2, float& b2, float& u2,
+                                              float& rd) {
+    const float dts = (float)sp + (r2 - r1);
+    rd = __fdividef(1.0f, dts);
+    u2 = (float)sp + r2;
+    // first bin: from u1 to its upper edge; last bin: from its lower edge to u2
+    const float h1 = 0.5f - r1, h2 = (float)sp - 0.5f + r2;
+    const float g2 = r2 + 0.5f, g1 = (float)sp - 0.5f - r1;
+    const float s1a = (1.0f + h2 * rd) * 0.5f * h1, s1b = h1 * rd * 0.5f * h1;
+    const float s2a = g2 * rd * 0.5f * g2, s2b = (1.0f + g1 * rd) * 0.5f * g2;
+    const bool spans = sp > 0;
+    a1 = !f ? 0.0f : spans ? s1a : 0.5f * dts;
+    b1 = !f ? 0.0f : spans ? s1b : 0.5f * dts;
+    a2 = f && spans ? s2a : 0.0f;
+    b2 = f && spans ? s2b : 0.0f;
+}
+
+__device__ __forceinline__ void deposit_multi2(const PointState2& p1, const PointState2& p2,
+                                               int Ba, int Bb, bool fa, bool fb, PairSink& sink) {
+    const int spa = fa ? p2.ka - p1.ka : 0, spb = fb ? p2.kb - p1.kb : 0;
+    float a1x, b1x, a2x, b2x, u2x, rdx, a1y, b1y, a2y, b2y, u2y, rdy;
+    multi_weights(fa, spa, p1.r.v.x, p2.r.v.x, a1x, b1x, a2x, b2x, u2x, rdx);
+    multi_weights(fb, spb, p1.r.v.y, p2.r.v.y, a1y, b1y, a2y, b2y, u2y, rdy);
+    sink.add_multi(fa, fb, Ba + p1.ka, Bb + p1.kb, spa, spb, p1.f, p2.f, f2(a1x, a1y), f2(b1x, b1y),
+                   f2(a2x, a2y), f2(b2x, b2y), p1.r, f2(u2x, u2y), f2(rdx, rdy));
 }
 
 // ---------------------------------------------------------------------------
@@ -511,7 +599,7 @@ struct PairShared {
 // One pixel tile (kPThreads pixels of the observer) against one slot of the
 // trajectory set: the whole work of a block of the per-observer kernel, and
 // one work item of the batched kernel.
-template <bool PINGPONG>
+template <bool PINGPONG, bool MULTI>
 __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
                                           const DevWork& wk, int slot, int tile,
                                           PairShared& sh) {
@@ -659,21 +747,35 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 const bool fast_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= 1u;
                 const bool fast_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= 1u;
                 bool go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a) && (!dep_b || fast_b));
+                bool out_a = false, out_b = false;
                 if (!go_fast) {
                     // steps that certainly lie outside the window add nothing
                     // and leave the fast path open
-                    const bool out_a = (q2.fla == 0 && A.Ba + q2.ka < 0) ||
-                                       (!(q1.fla & kExact) && A.Ba + q1.ka >= nt);
-                    const bool out_b = (q2.flb == 0 && A.Bb + q2.kb < 0) ||
-                                       (!(q1.flb & kExact) && A.Bb + q1.kb >= nt);
+                    out_a = (q2.fla == 0 && A.Ba + q2.ka < 0) ||
+                            (!(q1.fla & kExact) && A.Ba + q1.ka >= nt);
+                    out_b = (q2.flb == 0 && A.Bb + q2.kb < 0) ||
+                            (!(q1.flb & kExact) && A.Bb + q1.kb >= nt);
                     go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a || out_a) &&
                                                           (!dep_b || fast_b || out_b));
+                }
+                // regular steps that span up to kMaxSpan bins beyond their first
+                bool multi_a = false, multi_b = false, go_multi = false;
+                if constexpr (MULTI) {
+                    multi_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= (unsigned)kMaxSpan;
+                    multi_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= (unsigned)kMaxSpan;
+                    if (!go_fast)
+                        go_multi = __all_sync(0xffffffffu, (!dep_a || multi_a || out_a) &&
+                                                               (!dep_b || multi_b || out_b));
                 }
                 if (go_fast) {
                     const bool da = dep_a && fast_a, db = dep_b && fast_b;
                     // unconditional: a particle without a deposit adds zeros (its
                     // fields are finite for any observer off its trajectory)
                     deposit_fast2(q1, q2, A.Ba, A.Bb, da, db, sink);
+                    inwin += (unsigned)da + (unsigned)db;
+                } else if (go_multi) {
+                    const bool da = dep_a && multi_a, db = dep_b && multi_b;
+                    deposit_multi2(q1, q2, A.Ba, A.Bb, da, db, sink);
                     inwin += (unsigned)da + (unsigned)db;
                 } else {
                     if (dep_a) {
@@ -729,12 +831,15 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 // blocks are resident per SM (65536 / (32 MAXREG)): 128 -> 16, 136 -> 15,
 // 144 -> 14, 160 -> 13 (the unrolled loop needs ~152).  PINGPONG: the inner
 // loop unrolled by two with alternating point states (no copies, more
-// registers) or one step body with a copy per step.
-template <int MAXREG, bool PINGPONG>
+// registers) or one step body with a copy per step.  MULTI: warps whose
+// regular steps span up to kMaxSpan bins deposit them on packed pairs too
+// (instead of per particle); for observers whose bins are short against the
+// arrival advance of a step.  It costs ~1% where steps rarely span.
+template <int MAXREG, bool PINGPONG, bool MULTI = false>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
     __shared__ PairShared sh;
-    pair_tile<PINGPONG>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
+    pair_tile<PINGPONG, MULTI>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
 }
 
 // Persistent form: every block takes (observer, tile, slot) items from the
@@ -751,7 +856,7 @@ __global__ void __maxnreg__(MAXREG)
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= (unsigned int)n_items) break;
         const BatchItem bi = items[it];
-        pair_tile<false>(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile, sh);
+        pair_tile<false, false>(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile, sh);
         __syncwarp();
     }
 }
@@ -770,6 +875,9 @@ cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWo
         case kVariantPair144:
             lw_fp32_pair_kernel<144, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
             break;
+        case kVariantPairMulti:
+            lw_fp32_pair_kernel<128, false, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+            break;
         default:
             lw_fp32_pair_kernel<128, false><<<grid, kPThreads, 0, s>>>(tr, sc, w);
             break;
@@ -782,9 +890,9 @@ int pair_batch_blocks_per_sm() { return 65536 / (32 * kBatchMaxReg); }
 
 int pair_blocks_per_sm(int variant) {
     // occupancy of the kernel of each variant, asked once
-    static int cached[4] = {-1, -1, -1, -1};
+    static int cached[5] = {-1, -1, -1, -1, -1};
     const int k = variant == kVariantPair160 ? 1 : variant == kVariantPair136 ? 2
-                : variant == kVariantPair144 ? 3 : 0;
+                : variant == kVariantPair144 ? 3 : variant == kVariantPairMulti ? 4 : 0;
     if (cached[k] >= 0) return cached[k];
     int n = 0;
     cudaError_t e;
@@ -800,6 +908,10 @@ int pair_blocks_per_sm(int variant) {
         case 3:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<144, true>,
                                                               kPThreads, 0);
+            break;
+        case 4:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &n, lw_fp32_pair_kernel<128, false, true>, kPThreads, 0);
             break;
         default:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<128, false>,

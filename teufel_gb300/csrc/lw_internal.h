@@ -112,7 +112,9 @@ constexpr int kVariantPair = 3;
 constexpr int kVariantPair160 = 4;
 constexpr int kVariantPair136 = 5;
 constexpr int kVariantPair144 = 6;
-constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPair144; }
+// 16 resident warps per SM, with the packed deposit of steps spanning several bins
+constexpr int kVariantPairMulti = 7;
+constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPairMulti; }
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,

@@ -303,6 +303,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                         : opt.kernel_variant == 5 ? kVariantPair160
                         : opt.kernel_variant == 6 ? kVariantPair136
                         : opt.kernel_variant == 7 ? kVariantPair144
+                        : opt.kernel_variant == 8 ? kVariantPairMulti
                                                   : kVariantPair;  // 0 (automatic), 4
     const bool pairs = !fp64 && is_pair_variant(variant);
     // work units: particle segments, or pair segments for the pair kernel
@@ -880,7 +881,7 @@ int teufel_cuda_autotune(const teufel_traj_set* traj_c, const double* pix_pos,
     };
     // variants at the automatic slot count, then the best one at half and
     // twice as many slots; the first trial also loads the modules
-    const int variants[] = {4, 7, 6, 5, 1};
+    const int variants[] = {4, 7, 6, 5, 8, 1};
     float ms = 0.0f, best_t = 1e30f;
     int bv = 4, bp = 100, rc;
     if ((rc = trial(4, 100, &ms))) return cleanup(rc);
