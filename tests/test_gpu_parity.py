@@ -251,6 +251,34 @@ def test_uneven_particle_set(variant):
     assert rel_l2(g, ref) < TOL_FP32, rel_l2(g, ref)
 
 
+@pytest.mark.parametrize("variant", [4, 8])
+@pytest.mark.parametrize("dt", [2e-16, 3e-17, 1e-17])
+def test_steps_spanning_many_bins(c1, dt, variant):
+    """The single electron's steps advance the arrival time by ~0.3-0.8 fs.
+    With 0.2 fs bins they span 1-6 bins; with 30 as bins 11-39, so the
+    warps of variant 8 switch between its packed deposit (spans up to 16
+    beyond the first bin) and the general path; with 10 as bins 35-117, all
+    on the general path.  The window of every pixel (4096 bins) is centred on
+    the arrival from the trajectory's middle point."""
+    nt = 4096
+    C = 2.99792458e8
+    mid = c1.traj.t.shape[0] // 2
+    ts_mid = c1.traj.t[mid] + np.linalg.norm(c1.pix_pos - c1.traj.x[mid], axis=1) / C
+    t0 = ts_mid - 0.5 * nt * dt
+    ref, rc = lw.integrate_screen(c1.traj, c1.pix_pos, t0, dt, nt)
+    assert rc == 0 and np.abs(ref).max() > 0
+    with abi.TrajSet(c1.traj) as ts:
+        g = ts.integrate_screen(c1.pix_pos, t0, dt, nt, variant=variant)
+        inwin, _, st = ts.last_inwindow()
+        for p in (0, 220, 440):
+            idx, flags, _ = ts.point_decisions(0, c1.pix_pos[p], t0[p], dt, nt)
+            ri, rf = lw.point_decisions(c1.traj, 0, c1.pix_pos[p], t0[p], dt, nt)
+            assert np.array_equal(idx, ri)
+            assert np.array_equal(flags & 3, rf)
+    assert st == 0 and inwin > 0
+    assert rel_l2(g, ref) < TOL_FP32, rel_l2(g, ref)
+
+
 def test_charge_linearity(c1):
     """Doubling every charge doubles every trace sample exactly."""
     tr = c1.traj
