@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the FP32-vs-FP64 comparison on the other workloads")
+    ap.add_argument("--fp64-full", action="store_true",
+                    help="instead of the bench line: FP32 split against FP64 GPU on the full "
+                         "single-electron, 1e4-particle and gamma = 2000 workloads (~10 min)")
     return ap.parse_args()
 
 
@@ -243,6 +246,54 @@ def other_workloads():
                      "speedup_fp32_split_over_fp64": res["fp64"][1] / res["fp32"][1],
                      "rel_l2_fp32_split_vs_fp64":
                          float(np.linalg.norm(res["fp32"][0] - ref) / np.linalg.norm(ref))}
+    return out
+
+
+def full_comparison():
+    """FP32 split against the FP64 GPU path on three workloads in full: the
+    single electron on its 21x21 screen, the 1e4-particle 100 pC bunch on its
+    64x64 screen and the 1e3-particle gamma = 2000 bunch on its 100x100 screen
+    (8192 x 1 as).  Host buffers through integrate_screen, as a caller uses
+    it.  The FP64 path runs once (minutes) after a warm-up call on one pixel;
+    the FP32 path is tuned for the workload, then runs once as a warm-up and
+    best of three."""
+    from teufel_gb300 import abi, harness as H
+    out = {}
+    for name, make in (("single_electron_21x21_2048x5fs", H.config1),
+                       ("bunch_1e4_100pC_64x64_2048x5fs", H.config2),
+                       ("gamma2000_bunch_1e3_100x100_8192x1as", H.config5)):
+        tt = time.perf_counter()
+        w = make()
+        t_track = time.perf_counter() - tt
+        evals = w.n_pix * int(np.sum(np.maximum(w.traj.n_points.astype(np.int64) - 1, 0)))
+        with abi.TrajSet(w.traj) as ts:
+            ts.integrate_screen(w.pix_pos[:1], w.pix_t0[:1], w.dt, w.nots,
+                                precision=abi.PREC_FP64)
+            tt = time.perf_counter()
+            r64 = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=abi.PREC_FP64)
+            t64 = time.perf_counter() - tt
+            tv, _, _ = ts.autotune(w.pix_pos, w.pix_t0, w.dt, w.nots)
+            ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots)
+            t32 = None
+            for _ in range(3):
+                tt = time.perf_counter()
+                r32 = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots)
+                el = time.perf_counter() - tt
+                t32 = el if t32 is None else min(t32, el)
+            inwin, fallbacks, st = ts.last_inwindow()
+        diff = r32 - r64
+        out[name] = {"evals": evals, "pixels": w.n_pix, "particles": w.traj.n_particles,
+                     "samples": w.nots, "dt": w.dt, "in_window_fraction": inwin / evals,
+                     "exact_fallback_points": fallbacks, "status": st,
+                     "fp32_kernel": KERNEL_NAMES.get(tv, "?"),
+                     "fp32_split_s": t32, "fp64_gpu_s": t64,
+                     "fp32_split_evals_per_s": evals / t32, "fp64_gpu_evals_per_s": evals / t64,
+                     "speedup_fp32_split_over_fp64": t64 / t32,
+                     "rel_l2_fp32_split_vs_fp64":
+                         float(np.linalg.norm(diff) / np.linalg.norm(r64)),
+                     "peak_sample_rel_err": float(np.abs(diff).max() / np.abs(r64).max()),
+                     "tracking_s": t_track}
+        del r32, r64, diff
     return out
 
 
@@ -536,6 +587,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.fp64_full:
+        print(json.dumps({"fp32_split_vs_fp64_gpu_full_workloads": full_comparison()}))
+        return 0
     return run_gb300(args)
 
 
