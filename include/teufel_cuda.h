@@ -189,8 +189,10 @@ int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int
  * multi-bin deposits) at the automatic slot count,
  * then the fastest at half and twice as many slots, on these very inputs,
  * writing the trial traces to a scratch buffer (out-free: nothing is added
- * anywhere).  *best receives *opt with kernel_variant and n_slots set to the
- * winner, *best_ms (may be NULL) its time.  The choice is also remembered for
+ * anywhere).  A later candidate wins only when more than 0.5% faster than the
+ * best so far, so near-ties keep the default kernel and slot count.  *best
+ * receives *opt with kernel_variant and n_slots set to the winner, *best_ms
+ * (may be NULL) its time.  The choice is also remembered for
  * the shape class -- the log2 sizes of Np, Nt, the particle count and the
  * points per particle -- so later calls with kernel_variant = 0 on a similar
  * shape use it.  opt->device_pointers says where pix_pos/pix_t0 live.
