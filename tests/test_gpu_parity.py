@@ -279,6 +279,35 @@ def test_steps_spanning_many_bins(c1, dt, variant):
     assert rel_l2(g, ref) < TOL_FP32, rel_l2(g, ref)
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_buffer_call_equals_device_call(pinned):
+    """A host-buffer call with 403 MB of traces (64 particles on the full
+    64x64 screen, 2048 samples), whose trace buffer moves on the copy stream
+    (up during the integration, back in chunks behind the reduction), gives
+    the device-pointer call's traces bit for bit, added to what the caller's
+    buffer held; from pinned and from pageable host memory."""
+    import torch
+    w = H.config2(count=64)
+    rng = np.random.default_rng(5)
+    init = rng.standard_normal((w.n_pix, w.nots, 6)) * 1e-3
+    out_h = torch.from_numpy(init.copy())
+    out_h = (out_h.pin_memory() if pinned else out_h).numpy()
+    dev = torch.device("cuda", 0)
+    pos = torch.from_numpy(np.ascontiguousarray(w.pix_pos)).to(dev)
+    t0 = torch.from_numpy(np.ascontiguousarray(w.pix_t0)).to(dev)
+    out_d = torch.from_numpy(init).to(dev)
+    with abi.TrajSet(w.traj) as ts:
+        ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, out=out_h)
+        _, _, st = ts.last_inwindow()
+        assert st == 0
+        ts.integrate_screen_device(pos.data_ptr(), t0.data_ptr(), w.dt, w.nots, w.n_pix,
+                                   out_d.data_ptr())
+        torch.cuda.synchronize(dev)
+    g = out_d.cpu().numpy()
+    assert np.abs(g - init).max() > 0
+    assert np.array_equal(out_h, g)
+
+
 def test_charge_linearity(c1):
     """Doubling every charge doubles every trace sample exactly."""
     tr = c1.traj
