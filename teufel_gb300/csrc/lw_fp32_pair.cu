@@ -272,11 +272,17 @@ __device__ __forceinline__ PointState unpack(const PointState2& S) {
     return p;
 }
 
-// red.global.add.v2.f32 under a predicate: the L2 adds the pair when p holds.
-__device__ __forceinline__ void red_add2_if(bool p, float* addr, float a, float b) {
+// The six components of one bin, added by three red.global.add.v2.f32 under
+// one predicate: the L2 adds them when p holds.  One asm block, so the
+// predicate is formed once and the addresses are immediate offsets.
+__device__ __forceinline__ void red_add6_if(bool p, float* addr, float a0, float a1, float a2,
+                                            float a3, float a4, float a5) {
     asm volatile(
-        "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %0, 0;\n\t@q red.global.add.v2.f32 [%1], {%2, %3};\n\t}"
-        ::"r"((int)p), "l"(addr), "f"(a), "f"(b)
+        "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %0, 0;\n\t"
+        "@q red.global.add.v2.f32 [%1], {%2, %3};\n\t"
+        "@q red.global.add.v2.f32 [%1+8], {%4, %5};\n\t"
+        "@q red.global.add.v2.f32 [%1+16], {%6, %7};\n\t}"
+        ::"r"((int)p), "l"(addr), "f"(a0), "f"(a1), "f"(a2), "f"(a3), "f"(a4), "f"(a5)
         : "memory");
 }
 
@@ -425,11 +431,8 @@ struct PairSink {
             const bool pa = j < spa, pb = j < spb;
             float* qa = row + (int64_t)(ka + j) * 6;
             float* qb = row + (int64_t)(kb + j) * 6;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                red_add2_if(pa, qa + 2 * c, g[2 * c].v.x, g[2 * c + 1].v.x);
-                red_add2_if(pb, qb + 2 * c, g[2 * c].v.y, g[2 * c + 1].v.y);
-            }
+            red_add6_if(pa, qa, g[0].v.x, g[1].v.x, g[2].v.x, g[3].v.x, g[4].v.x, g[5].v.x);
+            red_add6_if(pb, qb, g[0].v.y, g[1].v.y, g[2].v.y, g[3].v.y, g[4].v.y, g[5].v.y);
         }
         open_a = sa ? ka + spa : open_a;
         open_b = sb ? kb + spb : open_b;
@@ -440,10 +443,8 @@ struct PairSink {
     }
     template <int W>
     __device__ __forceinline__ void reduce_if(bool p, int k) {
-        float* q = row + (int64_t)k * 6;
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-            red_add2_if(p, q + 2 * c, get<W>(2 * c), get<W>(2 * c + 1));
+        red_add6_if(p, row + (int64_t)k * 6, get<W>(0), get<W>(1), get<W>(2), get<W>(3),
+                    get<W>(4), get<W>(5));
     }
 };
 
