@@ -151,7 +151,10 @@ int64_t teufel_cuda_traj_points(const teufel_traj_set *traj);
  * Synchronous at return.  The work runs on s; out travels on a stream of the
  * set's own, ordered after the work already on s (up during the integration,
  * back in chunks behind the reduction), so pinned memory overlaps the copies
- * with the computation. */
+ * with the computation.  dt < 0 is accepted, as by the reference, and runs
+ * the FP64 kernel whatever the precision: the window is then reversed
+ * (tmin > tmax), and the reference either adds nothing or raises its range
+ * error (TEUFEL_ERR_RANGE) for a step straddling that window. */
 int teufel_cuda_integrate_screen(const teufel_traj_set *traj, const double *pix_pos,
                                  const double *pix_t0, double dt, int Nt, int Np, double *out,
                                  teufel_stream_t s);
@@ -210,7 +213,7 @@ typedef struct teufel_observer {
     const teufel_traj_set *traj;
     const double *pix_pos; /* [Np][3] */
     const double *pix_t0;  /* [Np]    */
-    double dt;
+    double dt;             /* > 0 for an observer with Np > 0 and Nt >= 2 */
     int Nt;
     int Np;
     double *out;           /* [Np][Nt][6], added into */
@@ -262,7 +265,7 @@ int teufel_cuda_batch_free(teufel_batch *batch);
  * TEUFEL_NOALLOC_SCRATCH_BYTES.
  *   d_pix_pos[Np][3], d_pix_t0[Np], d_out[Np][Nt][6]  device pointers; d_out is added into
  * Limit: Np*Nt*6*sizeof(float) must not exceed TEUFEL_NOALLOC_SCRATCH_BYTES,
- * otherwise TEUFEL_ERR_ARG is returned and nothing runs.  Larger observers
+ * otherwise TEUFEL_ERR_ARG is returned and nothing runs; dt must be > 0.  Larger observers
  * run in several passes of as many slots as fit.  Synchronous at return.
  * The array is shared by all calls and keeps the last call's contents (each
  * call clears what it uses first); calls that overlap on the GPU race.  The

@@ -71,7 +71,18 @@ def test_batch_matches_oracle_and_replays(screens):
 
 
 def test_batch_rejects_bad_arguments(screens):
+    import torch
     w = screens[1]
+    dev = torch.device("cuda", 0)
+    pos = torch.from_numpy(np.ascontiguousarray(w.pix_pos)).to(dev)
+    t0 = torch.from_numpy(np.ascontiguousarray(w.pix_t0)).to(dev)
+    out = torch.zeros((w.n_pix, w.nots, 6), dtype=torch.float64, device=dev)
     with abi.TrajSet(w.traj) as ts:
         with pytest.raises(abi.TeufelError):
             abi.Batch([(ts, 0, 0, w.dt, w.nots, w.n_pix, 0)])
+        # the batch runs FP32 kernels only: a reversed window (dt < 0) or dt = 0
+        for dt in (-w.dt, 0.0):
+            with pytest.raises(abi.TeufelError) as ei:
+                abi.Batch([(ts, pos.data_ptr(), t0.data_ptr(), dt, w.nots, w.n_pix,
+                            out.data_ptr())])
+            assert ei.value.status == abi.TEUFEL_ERR_ARG

@@ -352,6 +352,41 @@ def test_single_point_particles_are_skipped(c1):
     assert rel_l2(g, ref) < TOL_FP64
 
 
+@pytest.mark.parametrize("precision,variant", [(abi.PREC_FP64, 0), (abi.PREC_FP32_SPLIT, 4),
+                                               (abi.PREC_FP32_SPLIT, 1), (abi.PREC_FP32_SPLIT, 2)])
+def test_negative_bin_width(c1, precision, variant):
+    """dt < 0 is accepted, as by the reference, and then tmin = t0 - dt/2 lies
+    above tmax = t0 + dt (N - 1/2).  Only a step whose arrivals straddle that
+    reversed window passes the reference's window test, and its deposit goes
+    to a negative bin, which FieldTrace::add rejects (size_t index >= N): a
+    range error, as in the oracle.  A reversed window that holds a point's
+    arrival, or a long one, adds nothing."""
+    C = 2.99792458e8
+    sel = np.arange(0, c1.n_pix, 20)
+    mid = c1.traj.t.shape[0] // 2
+
+    def arrival(k):
+        return c1.traj.t[k] + np.linalg.norm(c1.pix_pos[sel] - c1.traj.x[k], axis=1) / C
+
+    cases = [(0.5 * (arrival(mid) + arrival(mid + 1)), -1e-17, 2),  # straddled: range error
+             (arrival(mid), -1e-17, 2),                             # holds an arrival: nothing
+             (c1.pix_t0[sel] + 2048 * 5e-15, -5e-15, 2048)]         # long: nothing
+    with abi.TrajSet(c1.traj) as ts:
+        for t0, dt, nt in cases:
+            ref, rc = lw.integrate_screen(c1.traj, c1.pix_pos[sel], t0, dt, nt)
+            if rc:
+                assert rc == abi.TEUFEL_ERR_RANGE
+                with pytest.raises(abi.TeufelError) as ei:
+                    ts.integrate_screen(c1.pix_pos[sel], t0, dt, nt, precision=precision,
+                                        variant=variant)
+                assert ei.value.status == abi.TEUFEL_ERR_RANGE
+            else:
+                assert not ref.any()
+                g = ts.integrate_screen(c1.pix_pos[sel], t0, dt, nt, precision=precision,
+                                        variant=variant)
+                assert not g.any()
+
+
 def test_non_finite_trajectory_rejected(c1):
     tr = c1.traj
     bad = H.Trajectories(tr.t.copy(), tr.x.copy(), tr.p.copy(), tr.a.copy(), tr.n_points,

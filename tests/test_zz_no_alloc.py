@@ -68,5 +68,8 @@ def test_noalloc_rejects_observers_beyond_the_array():
     out = torch.zeros((w.n_pix, nots, 6), dtype=torch.float64, device=dev)
     with abi.TrajSet(w.traj) as ts:
         st = noalloc(ts, pos, t0, w.dt, nots, w.n_pix, out)
+        # the warp kernel needs dt > 0 (a negative dt reverses the window)
+        st_neg = noalloc(ts, pos, t0, -w.dt, 16, w.n_pix, out)
     assert st == abi.TEUFEL_ERR_ARG
+    assert st_neg == abi.TEUFEL_ERR_ARG
     assert float(out.abs().max()) == 0.0

@@ -87,7 +87,9 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
                                                     const double* d_pix_t0, double dt, int Nt,
                                                     int Np, double* d_out, teufel_stream_t stream) {
     using namespace teufel;
-    if (!traj || Nt < 0 || Np < 0 || !(dt > 0.0 || dt < 0.0)) return TEUFEL_ERR_ARG;
+    // the warp kernel needs dt > 0 (a negative dt reverses the trace window;
+    // teufel_cuda_integrate_screen takes it)
+    if (!traj || Nt < 0 || Np < 0 || !(dt > 0.0)) return TEUFEL_ERR_ARG;
     if (Np > 0 && Nt > 0 && (!d_pix_pos || !d_pix_t0 || !d_out)) return TEUFEL_ERR_ARG;
     unsigned int* d_status = nullptr;
     const DevTraj* tr = traj_device_view(traj, &d_status);

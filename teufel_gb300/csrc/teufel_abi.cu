@@ -287,7 +287,13 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
                int slot_pct = 100, const HostOut* ho = nullptr) {
     teufel_options opt = opt_in;
-    const bool fp64 = opt.precision == TEUFEL_PREC_FP64;
+    // dt < 0 reverses the reference's window (tmin = t0 - dt/2 > tmax): a
+    // step then deposits only when its arrivals straddle that window, and
+    // the deposit goes to a negative bin, which FieldTrace::add rejects
+    // (src/particle.cpp:780-823, src/fieldtrace.cpp:185-190).  The FP64
+    // kernel takes exactly the reference's decisions there (no deposit, or
+    // the range error); the FP32 kernels assume dt > 0.
+    const bool fp64 = opt.precision == TEUFEL_PREC_FP64 || dt < 0.0;
     if (!fp64 && opt.kernel_variant == 0) {
         // automatic: a tuned choice for this shape class, if there is one
         std::lock_guard<std::mutex> lk(g_tune_mu);

@@ -85,7 +85,10 @@ int teufel_cuda_batch_create(int n_obs, const teufel_observer* obs, const teufel
     if (opt->precision != TEUFEL_PREC_FP32_SPLIT || !opt->device_pointers) return TEUFEL_ERR_ARG;
     for (int o = 0; o < n_obs; o++) {
         const teufel_observer& ob = obs[o];
+        // the batch runs FP32 kernels, which need dt > 0 (a negative dt
+        // reverses the trace window; teufel_cuda_integrate_screen takes it)
         if (!ob.traj || ob.Nt < 0 || ob.Np < 0 || !std::isfinite(ob.dt)) return TEUFEL_ERR_ARG;
+        if (ob.Np > 0 && ob.Nt >= 2 && !(ob.dt > 0.0)) return TEUFEL_ERR_ARG;
         if (ob.Np > 0 && ob.Nt > 0 && (!ob.pix_pos || !ob.pix_t0 || !ob.out))
             return TEUFEL_ERR_ARG;
     }
