@@ -154,7 +154,9 @@ int64_t teufel_cuda_traj_points(const teufel_traj_set *traj);
  * with the computation.  dt < 0 is accepted, as by the reference, and runs
  * the FP64 kernel whatever the precision: the window is then reversed
  * (tmin > tmax), and the reference either adds nothing or raises its range
- * error (TEUFEL_ERR_RANGE) for a step straddling that window. */
+ * error (TEUFEL_ERR_RANGE) for a step straddling that window.  So does a set
+ * with a particle whose arrival times can fall along its points (a step
+ * backwards in time, or a chord not slower than light). */
 int teufel_cuda_integrate_screen(const teufel_traj_set *traj, const double *pix_pos,
                                  const double *pix_t0, double dt, int Nt, int Np, double *out,
                                  teufel_stream_t s);
@@ -213,7 +215,9 @@ typedef struct teufel_observer {
     const teufel_traj_set *traj;
     const double *pix_pos; /* [Np][3] */
     const double *pix_t0;  /* [Np]    */
-    double dt;             /* > 0 for an observer with Np > 0 and Nt >= 2 */
+    double dt;             /* > 0 for an observer with Np > 0 and Nt >= 2; the set
+                              must have increasing arrival times (every step
+                              forward in time and slower than light) */
     int Nt;
     int Np;
     double *out;           /* [Np][Nt][6], added into */
@@ -265,7 +269,8 @@ int teufel_cuda_batch_free(teufel_batch *batch);
  * TEUFEL_NOALLOC_SCRATCH_BYTES.
  *   d_pix_pos[Np][3], d_pix_t0[Np], d_out[Np][Nt][6]  device pointers; d_out is added into
  * Limit: Np*Nt*6*sizeof(float) must not exceed TEUFEL_NOALLOC_SCRATCH_BYTES,
- * otherwise TEUFEL_ERR_ARG is returned and nothing runs; dt must be > 0.  Larger observers
+ * otherwise TEUFEL_ERR_ARG is returned and nothing runs; dt must be > 0 and
+ * every step of the set forward in time and slower than light.  Larger observers
  * run in several passes of as many slots as fit.  Synchronous at return.
  * The array is shared by all calls and keeps the last call's contents (each
  * call clears what it uses first); calls that overlap on the GPU race.  The

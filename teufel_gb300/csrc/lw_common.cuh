@@ -79,13 +79,25 @@ __device__ __forceinline__ double approx_retarded_time(const double4_32a tx, con
 // first and last step that may overlap [tmin, tmax]; an empty range has
 // first > last.  Widened by two steps on each side against rounding; the
 // per-step exact decisions then select exactly the reference's steps.
+// min_inc: the particle's smallest arrival advance of a step (vhat.w).  The
+// bisection needs the computed arrival times to increase along the points;
+// they do when that advance exceeds their rounding, checked here against 64
+// ulps of the arrival times at the ends of the range (all others lie between
+// them).  Otherwise the whole range is returned.
 __device__ __forceinline__ void inwindow_steps(const double4_32a* tx, int st_lo, int st_hi,
-                                               const double3 obs, const Window& w, int* first,
-                                               int* last) {
+                                               const double3 obs, const Window& w,
+                                               double min_inc, int* first, int* last) {
+    const double ts_lo = approx_retarded_time(tx[st_lo], obs);
+    const double ts_hi = approx_retarded_time(tx[st_hi], obs);
+    if (!(min_inc > 64.0 * 2.220446049250313e-16 * fmax(fabs(ts_lo), fabs(ts_hi)))) {
+        *first = st_lo;
+        *last = st_hi - 1;
+        return;
+    }
     // first point with ts > tmin in [st_lo, st_hi]; one evaluation when the
     // window opens before the range does
     int lo = st_lo, hi = st_hi + 1;
-    if (approx_retarded_time(tx[st_lo], obs) > w.tmin) hi = lo;
+    if (ts_lo > w.tmin) hi = lo;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
         if (approx_retarded_time(tx[mid], obs) > w.tmin) hi = mid; else lo = mid + 1;
@@ -95,7 +107,7 @@ __device__ __forceinline__ void inwindow_steps(const double4_32a* tx, int st_lo,
     // window closes after the range does
     lo = st_lo - 1;
     hi = st_hi;
-    if (approx_retarded_time(tx[st_hi], obs) < w.tmax) lo = hi;
+    if (ts_hi < w.tmax) lo = hi;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (approx_retarded_time(tx[mid], obs) < w.tmax) lo = mid; else hi = mid - 1;

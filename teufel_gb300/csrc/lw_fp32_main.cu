@@ -44,31 +44,34 @@ namespace teufel {
 // ---------------------------------------------------------------------------
 // Per-point preparation (pixel independent), run once after upload
 // ---------------------------------------------------------------------------
-// One warp per particle: the lanes test the steps in parallel.
+// One warp per particle: the lanes test the steps in parallel.  vhat.w is
+// the particle's smallest arrival advance of a step, min(dt - |dx|/c) > 0:
+// every observer's arrival time then grows by at least that much per step
+// (triangle inequality), which the range bisection relies on.  It is 0 when
+// some step does not run forward in time or is not slower than light, and
+// 1e300 for a particle without steps.
 __global__ void prep_particles_kernel(DevTraj tr, double4_32a* vhat) {
     const int m = blockIdx.x;
     if (m >= tr.n_particles) return;
     const int64_t o = tr.offsets[m], n = tr.offsets[m + 1] - o;
-    // Arrival times increase along the trajectory for every observer when
-    // time increases and every chord is slower than light (triangle
-    // inequality); the range bisection relies on it.
-    bool mono = true;
+    double min_inc = 1e300;
     for (int64_t i = o + threadIdx.x; i + 1 < o + n; i += 32) {
         const double4_32a p = tr.tx[i], q = tr.tx[i + 1];
         const double ddt = q.x - p.x;
         const double ex = q.y - p.y, ey = q.z - p.z, ez = q.w - p.w;
-        const double cd = kC * ddt;
-        mono = mono && (ddt > 0.0) && (ex * ex + ey * ey + ez * ez < 0.999999 * cd * cd);
+        const double inc = ddt - sqrt(ex * ex + ey * ey + ez * ez) / kC;
+        min_inc = (ddt > 0.0 && inc > 0.0) ? fmin(min_inc, inc) : 0.0;
     }
-    mono = __all_sync(0xffffffffu, mono);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) min_inc = fmin(min_inc, __shfl_xor_sync(0xffffffffu, min_inc, d));
     if (threadIdx.x != 0) return;
-    double4_32a v = make_double4_32a(0.0, 0.0, 1.0, 0.0);
+    double4_32a v = make_double4_32a(0.0, 0.0, 1.0, 1e300);
     if (n >= 2) {
         const double4_32a a = tr.tx[o], b = tr.tx[o + n - 1];
         const double dx = b.y - a.y, dy = b.z - a.z, dz = b.w - a.w;
         const double L = sqrt(dx * dx + dy * dy + dz * dz);
         if (L > 0.0) v = make_double4_32a(dx / L, dy / L, dz / L, 0.0);
-        v.w = mono ? 1.0 : 0.0;
+        v.w = min_inc;
     }
     vhat[m] = v;
 }
@@ -179,7 +182,8 @@ __global__ void __launch_bounds__(128, 4)
         if (st_hi > npm - 1) st_hi = npm - 1;
         if (st_lo >= st_hi) continue;  // uniform over the block
         int first = st_lo, last = st_hi - 1;
-        if (tr.vhat[m].w != 0.0) inwindow_steps(tr.tx + po, st_lo, st_hi, P, px.w, &first, &last);
+        if (tr.vhat[m].w > 0.0)
+            inwindow_steps(tr.tx + po, st_lo, st_hi, P, px.w, tr.vhat[m].w, &first, &last);
         if (!active) last = first - 1;
         int start = first & ~(kSegLen - 1);
         if (start < st_lo) start = st_lo;

@@ -572,8 +572,9 @@ __device__ __forceinline__ void particle_range(const DevTraj& tr, int m, int st_
     if (!active || st_lo >= st_hi) return;
     first = st_lo;
     last = st_hi - 1;
-    if (tr.vhat[m].w != 0.0)
-        inwindow_steps(tr.tx + tr.offsets[m], st_lo, st_hi, px.P, px.w, &first, &last);
+    if (tr.vhat[m].w > 0.0)
+        inwindow_steps(tr.tx + tr.offsets[m], st_lo, st_hi, px.P, px.w, tr.vhat[m].w, &first,
+                       &last);
     if (last < first) {
         first = 0x7fffffff;
         last = -1;

@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(kWThreads, MINB)
         if (st_hi > npm - 1) st_hi = npm - 1;
         if (st_lo >= st_hi) continue;  // uniform over the block
         int first = st_lo, last = st_hi - 1;
-        if (tr.vhat[m].w != 0.0) inwindow_steps(tr.tx + po, st_lo, st_hi, P, px.w, &first, &last);
+        if (tr.vhat[m].w > 0.0)
+            inwindow_steps(tr.tx + po, st_lo, st_hi, P, px.w, tr.vhat[m].w, &first, &last);
         if (!active || last < first) {
             first = 0x7fffffff;
             last = -1;

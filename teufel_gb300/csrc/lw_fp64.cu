@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(128)
         if (st_hi > npm - 1) st_hi = npm - 1;
         if (st_lo >= st_hi || !active) continue;
         int first = st_lo, last = st_hi - 1;
-        if (tr.vhat[m].w != 0.0) inwindow_steps(tr.tx + po, st_lo, st_hi, P, w, &first, &last);
+        if (tr.vhat[m].w > 0.0)
+            inwindow_steps(tr.tx + po, st_lo, st_hi, P, w, tr.vhat[m].w, &first, &last);
         if (last < first) continue;
         const double scale = field_scale(tr.charge[m]);
         Point64 p1, p2;

@@ -45,7 +45,9 @@ struct DevTraj {
     const int64_t* offsets;     // [n+1] first point of each particle
     const int64_t* seg_offsets; // [n+1] first segment of each particle
     const double* charge;       // [n] Coulomb
-    const double4_32a* vhat;        // [n] frame direction of each particle (mean velocity), w = monotone flag
+    const double4_32a* vhat;        // [n] frame direction of each particle (mean velocity);
+                                    // w = smallest arrival advance of a step, min(dt - |dx|/c),
+                                    // 0 when some step is not forward in time and slower than c
     const double4_32a* tx;          // [Npts] t, x, y, z                 (FP64, as uploaded)
     const double4_32a* pp;          // [Npts] beta*gamma, w unused        (FP64)
     const double4_32a* aa;          // [Npts] d(beta*gamma)/dt, w unused  (FP64)
@@ -56,8 +58,8 @@ struct DevTraj {
                                 //        1 - |chord velocity|/c
     // Particles 2j and 2j+1 form pair j (the last pair of an odd set has one
     // particle).  A pair is as long as its longer particle; its per-point
-    // data interleaves the two particles' q0..q3 component by component,
-    // 8 float4 per pair-point:
+    // data interleaves the two particles' q0..q2 and the chord offsets
+    // component by component, kPairPoint float4 per pair-point, e.g.:
     //   (e.x a, e.x b, e.y a, e.y b) (e.z a, e.z b, dt a, dt b)
     //   (bx a, bx b, by a, by b)     (bz a, bz b, eps a, eps b)
     //   (cx a, cx b, cy a, cy b)     (cz a, cz b, cw a, cw b)
@@ -65,6 +67,10 @@ struct DevTraj {
     // where b = beta-hat, c = q2, ch = chord direction; beyond the end of the
     // shorter particle its last point is repeated.
     Frame frame;
+    // 1 when some particle's arrival times can fall along its points (a step
+    // backwards in time or not slower than light): the set then runs on the
+    // FP64 kernel, whose decisions are the reference's for any step
+    int non_monotone;
     int n_pairs;
     int64_t n_pair_segments;
     const int64_t* pair_offsets;      // [n_pairs+1] first pair-point of each pair

@@ -93,6 +93,8 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
     if (Np > 0 && Nt > 0 && (!d_pix_pos || !d_pix_t0 || !d_out)) return TEUFEL_ERR_ARG;
     unsigned int* d_status = nullptr;
     const DevTraj* tr = traj_device_view(traj, &d_status);
+    // nor a set whose arrival times can fall along the points (FP64 only)
+    if (tr->non_monotone) return TEUFEL_ERR_ARG;
     // as the reference: no work for traces shorter than 2 samples or without steps
     if (Nt < 2 || Np == 0 || tr->n_particles == 0 || tr->n_segments == 0) return TEUFEL_OK;
     // one slot's partial traces must fit into the static array

@@ -292,8 +292,10 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     // the deposit goes to a negative bin, which FieldTrace::add rejects
     // (src/particle.cpp:780-823, src/fieldtrace.cpp:185-190).  The FP64
     // kernel takes exactly the reference's decisions there (no deposit, or
-    // the range error); the FP32 kernels assume dt > 0.
-    const bool fp64 = opt.precision == TEUFEL_PREC_FP64 || dt < 0.0;
+    // the range error); the FP32 kernels assume dt > 0.  The same holds for
+    // sets whose arrival times can fall along a particle's points (a step
+    // backwards in time or not slower than light, DevTraj::non_monotone).
+    const bool fp64 = opt.precision == TEUFEL_PREC_FP64 || dt < 0.0 || h->dev.non_monotone;
     if (!fp64 && opt.kernel_variant == 0) {
         // automatic: a tuned choice for this shape class, if there is one
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -462,11 +464,14 @@ Frame identity_frame() {
 // arithmetic untouched.
 cudaError_t set_frame(DevTraj& d) {
     d.frame = identity_frame();
+    d.non_monotone = 0;
     if (d.n_particles == 0) return cudaSuccess;
     std::vector<double4_32a> v((size_t)d.n_particles);
     cudaError_t e = cudaMemcpy(v.data(), d.vhat, sizeof(double4_32a) * v.size(),
                                cudaMemcpyDeviceToHost);
     if (e) return e;
+    for (const auto& q : v)
+        if (!(q.w > 0.0)) d.non_monotone = 1;
     double n[3] = {0.0, 0.0, 0.0};
     for (const auto& q : v) {
         n[0] += q.x;

@@ -89,6 +89,8 @@ int teufel_cuda_batch_create(int n_obs, const teufel_observer* obs, const teufel
         // reverses the trace window; teufel_cuda_integrate_screen takes it)
         if (!ob.traj || ob.Nt < 0 || ob.Np < 0 || !std::isfinite(ob.dt)) return TEUFEL_ERR_ARG;
         if (ob.Np > 0 && ob.Nt >= 2 && !(ob.dt > 0.0)) return TEUFEL_ERR_ARG;
+        // nor sets whose arrival times can fall along the points
+        if (traj_device_view(ob.traj, nullptr)->non_monotone) return TEUFEL_ERR_ARG;
         if (ob.Np > 0 && ob.Nt > 0 && (!ob.pix_pos || !ob.pix_t0 || !ob.out))
             return TEUFEL_ERR_ARG;
     }
