@@ -287,7 +287,10 @@ int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set *traj, const doub
  * round((ts-t0)/dt) clamped to [-2, Nt+1], flags bit0 = (ts <= tmin),
  * bit1 = (ts < tmax), bit2 = resolved by the exact FP64 fallback; and u_est,
  * the FP32-path estimate of (ts-t0)/dt.  The same device functions as the
- * main FP32 kernel are used.  Arrays have n_points[m] entries (host memory). */
+ * main FP32 kernel are used, so this is the FP32 path's decision; sets whose
+ * arrival times can fall along the points, and dt < 0, run on the FP64
+ * kernel instead, whose decisions are the reference's.  Arrays have
+ * n_points[m] entries (host memory). */
 int teufel_cuda_point_decisions(const teufel_traj_set *traj, int m, const double *pos, double t0,
                                 double dt, int Nt, int64_t *idx, int *flags, double *u_est,
                                 float *band);
