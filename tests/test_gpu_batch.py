@@ -71,7 +71,6 @@ def test_batch_matches_oracle_and_replays(screens):
 
 
 def test_batch_rejects_bad_arguments(screens):
-    import torch
     w = screens[1]
     dev = torch.device("cuda", 0)
     pos = torch.from_numpy(np.ascontiguousarray(w.pix_pos)).to(dev)
