@@ -125,3 +125,42 @@ def test_diffraction_screen_kat():
     same(traces[d["pix"]], d["traces"])
     np.testing.assert_allclose(flux, d["flux"], rtol=0, atol=1e-12 * np.abs(d["flux"]).max())
     np.testing.assert_allclose(energy, float(d["energy"]), rtol=1e-12)
+
+
+def test_oracle_equals_reference_on_unusual_inputs():
+    """The inputs the device routes to its FP64 kernel, pinned here: a
+    negative dt (a reversed window: a range error where a step straddles it,
+    nothing otherwise) and trajectories whose arrival times fall along the
+    points (the electron's points reversed; its positions doubled, chords
+    faster than light).  Same status as the reference's compiled
+    integrateFieldTrace, and the same traces where it raises nothing."""
+    if not lw.reference_available():
+        pytest.skip("the reference build oracle/_ref is not present on this machine")
+    w = H.config1()
+    tr = w.traj
+    sel = np.arange(0, w.n_pix, 20)
+    pos = w.pix_pos[sel]
+    C = 2.99792458e8
+    mid = tr.t.shape[0] // 2
+
+    def arrival(k):
+        return tr.t[k] + np.linalg.norm(pos - tr.x[k], axis=1) / C
+
+    reversed_ = H.Trajectories(tr.t[::-1].copy(), tr.x[::-1].copy(), tr.p[::-1].copy(),
+                               tr.a[::-1].copy(), tr.n_points, tr.charge, tr.mass)
+    doubled = H.Trajectories(tr.t.copy(), 2.0 * tr.x, tr.p.copy(), tr.a.copy(), tr.n_points,
+                             tr.charge, tr.mass)
+    cases = [(tr, 0.5 * (arrival(mid) + arrival(mid + 1)), -1e-17, 2),
+             (tr, arrival(mid), -1e-17, 2),
+             (tr, w.pix_t0[sel] + 2048 * 5e-15, -5e-15, 2048),
+             (reversed_, w.pix_t0[sel], w.dt, w.nots),
+             (doubled, w.pix_t0[sel], w.dt, w.nots)]
+    statuses = []
+    for t, t0, dt, nt in cases:
+        a, rc1 = lw.integrate_screen(t, pos, t0, dt, nt)
+        b, rc2 = lw.integrate_screen(t, pos, t0, dt, nt, impl="reference")
+        assert rc1 == rc2
+        statuses.append(rc1)
+        if rc1 == 0:
+            same(a, b)
+    assert statuses == [4, 0, 0, 0, 0]
