@@ -532,6 +532,21 @@ def run_gb300(args):
 
     if rank == 0:
         frac_in = inwin / (evals_step * K) if K else 0.0
+        # the metric's own qualifiers (accuracy against the FP64 GPU path and
+        # the speed-up over it) go into config, whose keys the line keeps
+        headline = {
+            "rel_l2_fp32_split_vs_fp64": rel, "peak_sample_rel_err_vs_fp64": peak_err,
+            "fp64_gpu_evals_per_s": fp64_rate, "fp32_split_evals_per_s_same_sample": fp32_rate_sub,
+            "speedup_fp32_split_over_fp64": fp32_rate_sub / fp64_rate,
+            "accuracy_sample": f"{len(sub)} pixels (every 16th) x {args.batch} particles",
+        }
+        if others:
+            headline["other_workloads"] = {
+                k.split("_")[0] + "_" + k.split("_")[1]: {
+                    "speedup_fp32_split_over_fp64": v["speedup_fp32_split_over_fp64"],
+                    "rel_l2_fp32_split_vs_fp64": v["rel_l2_fp32_split_vs_fp64"],
+                    "fp32_split_evals_per_s": v["fp32_split_evals_per_s"]}
+                for k, v in others.items()}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True,
@@ -543,7 +558,8 @@ def run_gb300(args):
                                        "in_window_fraction": frac_in,
                                        "point_evaluations_per_in_window_step":
                                            evaluations / inwin if inwin else None,
-                                       "exact_fallback_points": fallbacks}),
+                                       "exact_fallback_points": fallbacks,
+                                       "fp32_vs_fp64": headline}),
             "fp64_gpu": {"value": fp64_rate, "unit": UNIT,
                          "sample": f"{len(sub)} pixels (every 16th) x {args.batch} particles",
                          "fp32_split_same_sample": fp32_rate_sub,
@@ -566,13 +582,16 @@ def run_gb300(args):
                          "algorithmic_flops": flops, "kernel_ms": kernel_ms,
                          "reduce_ms": reduce_ms, "fp64_probe_tflops": peak64},
             "autotune": tuned,
-            "other_workloads": others,
             "batched_observers": batch,
             "gpu_launches": launches,
             "clocks": clk,
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
+        # the full comparison on the other workloads on a line of its own
+        # (stderr), so that it cannot push the bench line out of a log's tail
+        if others:
+            print(json.dumps({"other_workloads": others}), file=sys.stderr)
         print(json.dumps(line))
     for s in sets:
         s.free()

@@ -73,6 +73,13 @@ typedef struct teufel_options {
                              span several bins (short bins)                  */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
+    int max_device_mib;   /* upper bound on the device memory one call may take
+                             for its work buffers (staged pixels and traces of a
+                             host-buffer call, partial traces) [MiB]; 0 = none:
+                             partial traces then take up to 40% of the free
+                             memory.  Slots beyond the bound run as successive
+                             passes; a call that cannot run one slot within it
+                             returns TEUFEL_ERR_NOMEM before touching out.    */
 } teufel_options;
 
 /* Fill *opt with the defaults (FP32 split path, host pointers, automatic tiling). */
@@ -274,8 +281,10 @@ int teufel_cuda_batch_free(teufel_batch *batch);
  * run in several passes of as many slots as fit.  Synchronous at return.
  * The array is shared by all calls and keeps the last call's contents (each
  * call clears what it uses first); calls that overlap on the GPU race.  The
- * first call on a device looks the array's address up on that device, so it
- * should come before any stream capture. */
+ * first call on a device looks the array's address up on that device.  Every
+ * call waits for its stream s (after each pass and before it returns), so it
+ * must not be called while s, or any stream it would wait on, is being
+ * captured into a CUDA graph. */
 int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set *traj, const double *d_pix_pos,
                                          const double *d_pix_t0, double dt, int Nt, int Np,
                                          double *d_out, teufel_stream_t s);
@@ -294,6 +303,30 @@ int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set *traj, const doub
 int teufel_cuda_point_decisions(const teufel_traj_set *traj, int m, const double *pos, double t0,
                                 double dt, int Nt, int64_t *idx, int *flags, double *u_est,
                                 float *band);
+
+/* The decisions the shipping FP32 kernels take, recorded by their recording
+ * instantiations (the same source compiled with one more store per point).
+ * Runs teufel_cuda_integrate_screen_ex with host buffers on kernel variant 4
+ * (the default, also for 0) or 8 (opt->kernel_variant; opt->n_slots is
+ * honoured; opt may be NULL) and adds the traces into out[Np][Nt][6].
+ * rec[Np][n_particles][max_points] (host, max_points = the longest particle's
+ * point count) receives, for every point a kernel evaluated for a pixel as
+ * part of a particle's steps, its decision: (bin index round((ts-t0)/dt)
+ * clamped to [-2, Nt+1]) + 4 in bits 0-26, the flags of
+ * teufel_cuda_point_decisions in bits 27-29, bit 30 set when one point got two
+ * different decisions (the last point of a slot is evaluated again as the
+ * first of the next); 0 where no decision was taken.  Needs dt > 0 and
+ * increasing arrival times (the FP32 kernels' domain); synchronous. */
+int teufel_cuda_record_decisions(const teufel_traj_set *traj, const double *pix_pos,
+                                 const double *pix_t0, double dt, int Nt, int Np,
+                                 const teufel_options *opt, int32_t *rec, double *out);
+
+/* The same record for observer obs of a batch, taken by the recording
+ * instantiation of the persistent batched kernel: one run of the whole batch
+ * (every observer's out is added into, as by teufel_cuda_batch_run) in which
+ * observer obs records its decisions into rec[Np][n_particles][max_points]
+ * (host).  Synchronous. */
+int teufel_cuda_batch_record_decisions(teufel_batch *batch, int obs, int32_t *rec);
 
 /* Run the device deposit routine on injected arrival times and fields (the
  * reference's known-answer test, tests/teufel.integrate_field.cpp:51-78,

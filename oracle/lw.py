@@ -8,7 +8,6 @@ oracle/lw_oracle.c for what the restatement follows, file by line.
 from __future__ import annotations
 
 import ctypes
-import os
 import subprocess
 from pathlib import Path
 
@@ -27,11 +26,26 @@ _oracle = None
 _ref = None
 
 
+_ref_src_cache: list = []
+
+
+def reference_src():
+    """The reference's source directory, as oracle/Makefile finds it
+    (TEUFEL_REFERENCE_SRC, else the recipe's default location), or None when
+    the tree is absent (on the GPU machine it always is)."""
+    if not _ref_src_cache:
+        r = subprocess.run(["make", "-s", "-C", str(HERE), "refdir"], stdout=subprocess.PIPE,
+                           stderr=subprocess.DEVNULL, text=True)
+        d = r.stdout.strip() if r.returncode == 0 else ""
+        _ref_src_cache.append(Path(d) if d else None)
+    return _ref_src_cache[0]
+
+
 def build(with_reference: bool = True) -> None:
     """make -C oracle (and the reference build where its sources exist)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
-    src = Path(os.environ.get("TEUFEL_REFERENCE_SRC", "/root/reference/src"))
-    if with_reference and (src / "particle.cpp").exists():
+    src = reference_src() if with_reference else None
+    if src is not None:
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={src}"], check=True)
 
 
@@ -68,6 +82,9 @@ def oracle():
         L.lwo_retarded_field_at.restype = ctypes.c_int
         L.lwo_retarded_field_at.argtypes = [_i64, _lp, _dp, _dp, _dp, _dp, _dp, ctypes.c_double,
                                             _i64, _dp, _dp, ctypes.c_int]
+        L.lwo_screen_decisions.restype = None
+        L.lwo_screen_decisions.argtypes = [_i64, _lp, _dp, _dp, _i64, _dp, _dp, ctypes.c_double,
+                                           _i64, _i64, ctypes.POINTER(ctypes.c_int32)]
         L.lwo_step_decisions.restype = None
         L.lwo_step_decisions.argtypes = [_i64, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                          _i64, _lp, _lp, _bp]
@@ -183,6 +200,23 @@ def point_decisions(traj, m, obs, t0, dt, nots):
     return idx, fl
 
 
+def screen_decisions(traj, pix_pos, pix_t0, dt, nots):
+    """The reference's decision of every (pixel, particle, point) of a screen,
+    [n_pix, n_particles, max_points] int32 encoded as the device's decision
+    record: (bin index + 4) | (flags << 27), flags bit0 = ts <= tmin,
+    bit1 = ts < tmax; 0 beyond a particle's last point."""
+    pix_pos = _c(pix_pos)
+    pix_t0 = _c(pix_t0)
+    n_pix = pix_pos.shape[0]
+    stride = int(np.max(traj.n_points)) if traj.n_particles else 0
+    rec = np.zeros((n_pix, traj.n_particles, stride), dtype=np.int32)
+    offs = _c(traj.offsets, np.int64)
+    oracle().lwo_screen_decisions(traj.n_particles, _p(offs, _lp), _p(_c(traj.t)),
+                                  _p(_c(traj.x)), n_pix, _p(pix_pos), _p(pix_t0), dt, nots,
+                                  stride, _p(rec, ctypes.POINTER(ctypes.c_int32)))
+    return rec
+
+
 def step_decisions(traj, m, obs, t0, dt, nots):
     """Per step of particle m: (round((ts1-t0)/dt), round((ts2-t0)/dt), case)
     with case 0 = outside the window, 1 = starts before it, 2 = inside."""
@@ -217,7 +251,9 @@ def track_reference(init, lattice_packed, tstep, n_steps, charge, mass):
 def reference_file(rel: str):
     """Path of a file of the reference tree (rel to its root), or None where
     the tree is absent.  The tree is found beside its src/ directory."""
-    src = Path(os.environ.get("TEUFEL_REFERENCE_SRC", "/root/reference/src"))
+    src = reference_src()
+    if src is None:
+        return None
     f = src.parent / rel
     return f if f.exists() else None
 

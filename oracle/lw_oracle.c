@@ -340,6 +340,39 @@ void lwo_point_decisions(int64_t np, const double *t, const double *x, const dou
     }
 }
 
+/* The decisions of lwo_point_decisions for every (pixel, particle, point) of
+   a screen, encoded as the device's decision record does
+   (teufel_cuda_record_decisions): (idx + 4) | (flags << 27), at
+   rec[(pixel * n_particles + m) * stride + i].  OpenMP over pixels. */
+void lwo_screen_decisions(int64_t n_particles, const int64_t *offsets, const double *t,
+                          const double *x, int64_t n_pix, const double *pix_pos,
+                          const double *pix_t0, double dt, int64_t nots, int64_t stride,
+                          int32_t *rec)
+{
+    int64_t p;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (p = 0; p < n_pix; p++) {
+        const double *obs = pix_pos + 3 * p;
+        const double t0 = pix_t0[p];
+        const double tmin = t0 - dt * 0.5;
+        const double tmax = t0 + dt * ((double)nots - 0.5);
+        for (int64_t m = 0; m < n_particles; m++) {
+            int32_t *r = rec + (p * n_particles + m) * stride;
+            for (int64_t i = offsets[m]; i < offsets[m + 1]; i++) {
+                double ts = lwo_retarded_time(t[i], x + 3 * i, obs);
+                double u = (ts - t0) / dt;
+                if (u < -4.0) u = -4.0;
+                if (u > (double)nots + 4.0) u = (double)nots + 4.0;
+                int64_t k = (int64_t)round(u);
+                if (k < -2) k = -2;
+                if (k > nots + 1) k = nots + 1;
+                int32_t fl = (ts <= tmin ? 1 : 0) | (ts < tmax ? 2 : 0);
+                r[i - offsets[m]] = (int32_t)((k + 4) | ((int64_t)fl << 27));
+            }
+        }
+    }
+}
+
 /* Per-point decision record used by the bin-index parity tests: for each
    step of particle m at observer obs, the pair (round((ts1-t0)/dt),
    round((ts2-t0)/dt)) and the case (0 = outside, 1 = starts before the

@@ -36,7 +36,8 @@ EXPORTED = [
     "teufel_cuda_probe_peaks", "teufel_cuda_last_timing", "teufel_cuda_integrate_screen_noalloc",
     "teufel_cuda_batch_create", "teufel_cuda_batch_run", "teufel_cuda_batch_status",
     "teufel_cuda_batch_free", "teufel_cuda_autotune", "teufel_cuda_retarded_field",
-    "teufel_cuda_traj_track", "teufel_cuda_traj_download",
+    "teufel_cuda_traj_track", "teufel_cuda_traj_download", "teufel_cuda_record_decisions",
+    "teufel_cuda_batch_record_decisions",
 ]
 
 # bytes of the fixed device array used by teufel_cuda_integrate_screen_noalloc
@@ -46,7 +47,7 @@ NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("n_slots", ctypes.c_int), ("kernel_variant", ctypes.c_int),
-                ("timing", ctypes.c_int)]
+                ("timing", ctypes.c_int), ("max_device_mib", ctypes.c_int)]
 
 
 class ObserverDesc(ctypes.Structure):
@@ -160,6 +161,13 @@ def lib():
                                            ctypes.POINTER(Options), _dp]
         L.teufel_cuda_batch_free.restype = ctypes.c_int
         L.teufel_cuda_batch_free.argtypes = [_vp]
+        _i32p = ctypes.POINTER(ctypes.c_int32)
+        L.teufel_cuda_record_decisions.restype = ctypes.c_int
+        L.teufel_cuda_record_decisions.argtypes = [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.POINTER(Options), _i32p,
+                                                   _dp]
+        L.teufel_cuda_batch_record_decisions.restype = ctypes.c_int
+        L.teufel_cuda_batch_record_decisions.argtypes = [_vp, ctypes.c_int, _i32p]
         _lib = L
     return _lib
 
@@ -183,7 +191,8 @@ def _ptr(a, t=_dp):
 
 
 def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
-            n_slots: int = 0, timing: bool = False, variant: int = 0) -> Options:
+            n_slots: int = 0, timing: bool = False, variant: int = 0,
+            max_device_mib: int = 0) -> Options:
     o = Options()
     lib().teufel_cuda_default_options(ctypes.byref(o))
     o.precision = precision
@@ -191,6 +200,7 @@ def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
     o.n_slots = n_slots
     o.timing = 1 if timing else 0
     o.kernel_variant = variant
+    o.max_device_mib = max_device_mib
     return o
 
 
@@ -272,7 +282,8 @@ class TrajSet:
     # -- integration ----------------------------------------------------
     def integrate_screen(self, pix_pos, pix_t0, dt, nots, out=None,
                          precision: int = PREC_FP32_SPLIT, n_slots: int = 0,
-                         stream: int = 0, variant: int = 0) -> np.ndarray:
+                         stream: int = 0, variant: int = 0,
+                         max_device_mib: int = 0) -> np.ndarray:
         """Traces of all particles on the pixels, added into ``out``
         ([Np][nots][6] doubles, zeros if None) -- host buffers."""
         pix_pos = _c(pix_pos).reshape(-1, 3)
@@ -282,7 +293,7 @@ class TrajSet:
             out = np.zeros((n_pix, nots, 6))
         if not (out.dtype == np.float64 and out.flags.c_contiguous):
             raise ValueError("out must be a C-contiguous float64 array")
-        opt = options(precision, False, n_slots, variant=variant)
+        opt = options(precision, False, n_slots, variant=variant, max_device_mib=max_device_mib)
         check(lib().teufel_cuda_integrate_screen_ex(self.handle, pix_pos.ctypes.data,
                                                     pix_t0.ctypes.data, dt, nots, n_pix,
                                                     out.ctypes.data, ctypes.byref(opt),
@@ -357,6 +368,24 @@ class TrajSet:
                                          ctypes.byref(ms)), "teufel_cuda_autotune")
         return int(best.kernel_variant), int(best.n_slots), float(ms.value)
 
+    def record_decisions(self, pix_pos, pix_t0, dt, nots, variant: int = 4, n_slots: int = 0):
+        """teufel_cuda_record_decisions: (traces [Np][nots][6], decision record
+        [Np][n_particles][max points] int32) of the recording instantiation
+        of the shipping pair kernel (variant 4 or 8)."""
+        pix_pos = _c(pix_pos).reshape(-1, 3)
+        pix_t0 = _c(pix_t0).reshape(-1)
+        n_pix = pix_pos.shape[0]
+        out = np.zeros((n_pix, nots, 6))
+        stride = int(np.max(self.n_points)) if self.n_particles else 0
+        rec = np.zeros((n_pix, self.n_particles, stride), dtype=np.int32)
+        opt = options(PREC_FP32_SPLIT, False, n_slots, variant=variant)
+        check(lib().teufel_cuda_record_decisions(self.handle, _ptr(pix_pos), _ptr(pix_t0), dt,
+                                                 nots, n_pix, ctypes.byref(opt),
+                                                 _ptr(rec, ctypes.POINTER(ctypes.c_int32)),
+                                                 _ptr(out)),
+              "teufel_cuda_record_decisions")
+        return out, rec
+
     def point_decisions(self, m, pos, t0, dt, nots):
         n = int(self.n_points[m])
         idx = np.zeros(n, dtype=np.int64)
@@ -425,6 +454,17 @@ class Batch:
         st = lib().teufel_cuda_batch_status(self.handle, ctypes.byref(items), ctypes.byref(inw),
                                             ctypes.byref(ms))
         return st, int(items.value), int(inw.value), float(ms.value)
+
+    def record_decisions(self, obs: int, n_pix: int, traj_set) -> np.ndarray:
+        """teufel_cuda_batch_record_decisions: one run of the batch in which
+        observer `obs` (n_pix pixels, trajectory set traj_set) records its
+        decisions, [n_pix][n_particles][max points] int32."""
+        stride = int(np.max(traj_set.n_points)) if traj_set.n_particles else 0
+        rec = np.zeros((n_pix, traj_set.n_particles, stride), dtype=np.int32)
+        check(lib().teufel_cuda_batch_record_decisions(self.handle, obs,
+                                                       _ptr(rec, ctypes.POINTER(ctypes.c_int32))),
+              "teufel_cuda_batch_record_decisions")
+        return rec
 
     def close(self) -> None:
         if self.handle:

@@ -67,10 +67,16 @@ __device__ __forceinline__ int exact_flags(double ts, const Window& w) {
 }
 
 // Fast arrival-time estimate for range searches only (FMA, approximate sqrt):
-// within a few ulp of the exact value; callers widen ranges by two steps.
-__device__ __forceinline__ double approx_retarded_time(const double4_32a tx, const double3 obs) {
+// within a few ulp of the larger of its terms t and R/c; callers widen
+// ranges by two steps.  mag (optional) receives |t| + R/c, the scale of its
+// rounding: when t is close to -R/c (a negative emission time) the sum is
+// much smaller than its terms and carries their rounding, not its own.
+__device__ __forceinline__ double approx_retarded_time(const double4_32a tx, const double3 obs,
+                                                       double* mag = nullptr) {
     double rx = obs.x - tx.y, ry = obs.y - tx.z, rz = obs.z - tx.w;
     double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
+    const double rc = sqrt(r2) * (1.0 / kC);
+    if (mag) *mag = fabs(tx.x) + rc;
     return fma(sqrt(r2), 1.0 / kC, tx.x);
 }
 
@@ -82,14 +88,19 @@ __device__ __forceinline__ double approx_retarded_time(const double4_32a tx, con
 // min_inc: the particle's smallest arrival advance of a step (vhat.w).  The
 // bisection needs the computed arrival times to increase along the points;
 // they do when that advance exceeds their rounding, checked here against 64
-// ulps of the arrival times at the ends of the range (all others lie between
-// them).  Otherwise the whole range is returned.
+// ulps of the scale of their terms, |t| + R/c, at the ends of the range
+// (emission times and distances between those ends are bounded by theirs for
+// a forward, slower-than-light trajectory: |t| by the larger end, R/c by the
+// larger end plus the time between the ends).  Otherwise the whole range is
+// returned.
 __device__ __forceinline__ void inwindow_steps(const double4_32a* tx, int st_lo, int st_hi,
                                                const double3 obs, const Window& w,
                                                double min_inc, int* first, int* last) {
-    const double ts_lo = approx_retarded_time(tx[st_lo], obs);
-    const double ts_hi = approx_retarded_time(tx[st_hi], obs);
-    if (!(min_inc > 64.0 * 2.220446049250313e-16 * fmax(fabs(ts_lo), fabs(ts_hi)))) {
+    double mag_lo, mag_hi;
+    const double ts_lo = approx_retarded_time(tx[st_lo], obs, &mag_lo);
+    const double ts_hi = approx_retarded_time(tx[st_hi], obs, &mag_hi);
+    const double span = fabs(tx[st_hi].x - tx[st_lo].x);
+    if (!(min_inc > 64.0 * 2.220446049250313e-16 * (fmax(mag_lo, mag_hi) + span))) {
         *first = st_lo;
         *last = st_hi - 1;
         return;

@@ -448,6 +448,32 @@ struct PairSink {
     }
 };
 
+// The decision taken for point i of particle m (particle W of the pair) at
+// this lane's pixel: the exact evaluation's bin and flags where the point
+// fell back to it, else the bin B + ki and the window flags it implies (as
+// materialize does), into the decision record.  A point evaluated twice (the
+// last point of one slot is the first of the next) must get the same
+// decision both times; a difference is flagged.
+template <int W>
+__device__ __forceinline__ void record_point(const DevWork& wk, int n_particles, int pix, int m,
+                                             int i, const PointState2& q, int B, int nt) {
+    const int f = W ? q.flb : q.fla;
+    int idx, fl;
+    if (f & kExact) {
+        idx = W ? q.idxb : q.idxa;
+        fl = f;
+    } else {
+        int k = B + (W ? q.kb : q.ka);
+        k = k < -2 ? -2 : (k > nt + 1 ? nt + 1 : k);
+        idx = k;
+        fl = (k < 0 ? kLeTmin : 0) | (k < nt ? kLtTmax : 0);
+    }
+    const int v = rec_encode(idx, fl);
+    int* p = wk.rec + ((int64_t)pix * n_particles + m) * wk.rec_stride + i;
+    const int old = atomicCAS(p, 0, v);
+    if (old != 0 && old != v) atomicOr(p, kRecConflict);
+}
+
 template <int W>
 struct PairView {
     PairSink* s;
@@ -601,7 +627,7 @@ struct PairShared {
 // One pixel tile (kPThreads pixels of the observer) against one slot of the
 // trajectory set: the whole work of a block of the per-observer kernel, and
 // one work item of the batched kernel.
-template <bool PINGPONG, bool MULTI>
+template <bool PINGPONG, bool MULTI, bool REC>
 __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
                                           const DevWork& wk, int slot, int tile,
                                           PairShared& sh) {
@@ -746,6 +772,10 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                         atomicAdd(&sh.stats[1], 1ull);
                     }
                 }
+                if constexpr (REC) {
+                    if (i <= lim_a) record_point<0>(wk, tr.n_particles, pix, ma, i, q2, A.Ba, nt);
+                    if (i <= lim_b) record_point<1>(wk, tr.n_particles, pix, mb, i, q2, A.Bb, nt);
+                }
                 const bool fast_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= 1u;
                 const bool fast_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= 1u;
                 bool go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a) && (!dep_b || fast_b));
@@ -837,16 +867,20 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 // regular steps span up to kMaxSpan bins deposit them on packed pairs too
 // (instead of per particle); for observers whose bins are short against the
 // arrival advance of a step.  It costs ~1% where steps rarely span.
-template <int MAXREG, bool PINGPONG, bool MULTI = false>
+//
+// REC: the recording instantiation, which also writes every point decision it
+// takes into DevWork::rec (the parity tests compare them with the oracle's);
+// its arithmetic and decisions are those of the instantiation without it.
+template <int MAXREG, bool PINGPONG, bool MULTI = false, bool REC = false>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
     __shared__ PairShared sh;
-    pair_tile<PINGPONG, MULTI>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
+    pair_tile<PINGPONG, MULTI, REC>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
 }
 
 // Persistent form: every block takes (observer, tile, slot) items from the
 // queue until it is empty.
-template <int MAXREG>
+template <int MAXREG, bool REC = false>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_batch_kernel(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
                               const BatchItem* items, int n_items, unsigned int* head) {
@@ -858,7 +892,12 @@ __global__ void __maxnreg__(MAXREG)
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= (unsigned int)n_items) break;
         const BatchItem bi = items[it];
-        pair_tile<false, false>(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile, sh);
+        if (REC && wks[bi.obs].rec)
+            pair_tile<false, false, true>(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile,
+                                          sh);
+        else
+            pair_tile<false, false, false>(trs[bi.obs], scs[bi.obs], wks[bi.obs], bi.slot, bi.tile,
+                                           sh);
         __syncwarp();
     }
 }
@@ -867,6 +906,16 @@ __global__ void __maxnreg__(MAXREG)
 cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWork& w,
                              int variant, cudaStream_t s) {
     dim3 grid((sc.np + kPThreads - 1) / kPThreads, w.n_slots);
+    if (w.rec) {
+        // the recording instantiations of the kernels the automatic choice uses
+        if (variant == kVariantPairMulti)
+            lw_fp32_pair_kernel<128, false, true, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+        else if (variant == kVariantPair)
+            lw_fp32_pair_kernel<128, false, false, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+        else
+            return cudaErrorInvalidValue;
+        return cudaGetLastError();
+    }
     switch (variant) {
         case kVariantPair160:
             lw_fp32_pair_kernel<160, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
@@ -930,9 +979,13 @@ int pair_blocks_per_sm(int variant) {
 
 cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
                                    const BatchItem* items, int n_items, unsigned int* head,
-                                   int n_blocks, cudaStream_t s) {
-    lw_fp32_pair_batch_kernel<kBatchMaxReg><<<n_blocks, kPThreads, 0, s>>>(trs, scs, wks, items,
-                                                                          n_items, head);
+                                   int n_blocks, cudaStream_t s, bool record) {
+    if (record)
+        lw_fp32_pair_batch_kernel<kBatchMaxReg, true><<<n_blocks, kPThreads, 0, s>>>(
+            trs, scs, wks, items, n_items, head);
+    else
+        lw_fp32_pair_batch_kernel<kBatchMaxReg><<<n_blocks, kPThreads, 0, s>>>(trs, scs, wks, items,
+                                                                              n_items, head);
     return cudaGetLastError();
 }
 

@@ -99,7 +99,22 @@ struct DevWork {
     unsigned long long* counters;  // [0] in-window triples, [1] exact-fallback points,
                                    // [2] bin contributions (deposits), [3] point
                                    // evaluations (in window or walked for a neighbour)
+    // Decision record (the recording instantiations of the pair kernels only;
+    // nullptr otherwise): rec[(pixel * n_particles + m) * rec_stride + i] of
+    // point i of particle m receives the decision the kernel took for it,
+    // encoded by rec_encode.
+    int* rec;
+    int64_t rec_stride;
 };
+
+// A point decision as recorded: bin index + 4 in bits 0-26, the window and
+// exact flags (kLeTmin | kLtTmax | kExact) in bits 27-29; bit 30 marks two
+// different decisions recorded for one point.  0 means "not recorded".
+constexpr int kRecFlagShift = 27;
+constexpr int kRecConflict = 1 << 30;
+__host__ __device__ constexpr int rec_encode(int idx, int flags) {
+    return (idx + 4) | (flags << kRecFlagShift);
+}
 
 }  // namespace teufel
 
@@ -180,7 +195,7 @@ struct BatchItem {
 // The persistent batched kernel (pair kernel body) and the batched reduction.
 cudaError_t launch_fp32_pair_batch(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
                                    const BatchItem* items, int n_items, unsigned int* head,
-                                   int n_blocks, cudaStream_t s);
+                                   int n_blocks, cudaStream_t s, bool record = false);
 int pair_batch_blocks_per_sm();
 // resident one-warp blocks per SM of the pair kernel of a variant (0: unknown)
 int pair_blocks_per_sm(int variant);
@@ -194,4 +209,6 @@ struct teufel_traj_set;
 namespace teufel {
 // device view and status word of a trajectory handle (teufel_abi.cu)
 const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** status);
+// the longest particle's point count of a handle (the decision record's stride)
+int64_t traj_max_points(const teufel_traj_set* traj);
 }  // namespace teufel

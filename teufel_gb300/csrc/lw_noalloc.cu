@@ -21,10 +21,12 @@
 //
 // Set-up: the device address of the array is looked up once per device with
 // cudaGetSymbolAddress, with that device current, by the first call made on
-// that device; that first call should come before any stream capture.
+// that device.  Every call synchronizes its stream (after each pass and at the
+// end), so no call can be made while that stream is being captured.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <mutex>
 
@@ -89,7 +91,7 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
     using namespace teufel;
     // the warp kernel needs dt > 0 (a negative dt reverses the trace window;
     // teufel_cuda_integrate_screen takes it)
-    if (!traj || Nt < 0 || Np < 0 || !(dt > 0.0)) return TEUFEL_ERR_ARG;
+    if (!traj || Nt < 0 || Np < 0 || !std::isfinite(dt) || !(dt > 0.0)) return TEUFEL_ERR_ARG;
     if (Np > 0 && Nt > 0 && (!d_pix_pos || !d_pix_t0 || !d_out)) return TEUFEL_ERR_ARG;
     unsigned int* d_status = nullptr;
     const DevTraj* tr = traj_device_view(traj, &d_status);
@@ -137,6 +139,8 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
         w.status = d_status;
         w.frame = tr->frame;
         w.counters = nullptr;
+        w.rec = nullptr;
+        w.rec_stride = 0;
         e = launch_fp32(*tr, sc, w, kVariantUniform, s);
         if (!e) e = launch_reduce_fp32(w, sc, d_out, s);
         if (e) return fail(e);

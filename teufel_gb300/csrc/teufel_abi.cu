@@ -43,6 +43,7 @@ struct teufel_traj_set {
     int last_launches = 0;
     bool last_timed = false;
     std::vector<int64_t> h_seg_offsets;
+    int64_t max_points = 0;  // the longest particle's point count
     int last_slots = 0;
     bool counted = false;  // included in the live-set count of its device
     // host-buffer calls: a copy stream that moves the trace buffer while the
@@ -285,7 +286,8 @@ int64_t fill_waves(const teufel_traj_set* h, int np, int variant, int64_t slots)
 
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
                int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
-               int slot_pct = 100, const HostOut* ho = nullptr) {
+               int slot_pct = 100, const HostOut* ho = nullptr, int* d_rec = nullptr,
+               size_t staged_bytes = 0) {
     teufel_options opt = opt_in;
     // dt < 0 reverses the reference's window (tmin = t0 - dt/2 > tmax): a
     // step then deposits only when its arrivals straddle that window, and
@@ -336,6 +338,12 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     if (!pool) return TEUFEL_ERR_CUDA;
     size_t budget = std::min<size_t>((size_t)48 << 30,
                                      (size_t)(0.4 * (double)available_bytes(pool)));
+    if (opt.max_device_mib > 0) {
+        // the caller's bound, less what the call has staged already
+        const size_t cap = (size_t)opt.max_device_mib << 20;
+        if (cap < staged_bytes + slot_bytes) return TEUFEL_ERR_NOMEM;
+        budget = std::min(budget, cap - staged_bytes);
+    }
     int64_t per_pass = slot_bytes ? (int64_t)(budget / slot_bytes) : slots_total;
     per_pass = std::max<int64_t>(1, std::min<int64_t>(per_pass, slots_total));
     const size_t scratch_bytes = std::max<size_t>(slot_bytes * (size_t)per_pass, 256);
@@ -391,6 +399,8 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         w.status = h->d_status;
         w.frame = h->dev.frame;
         w.counters = h->d_counters;
+        w.rec = d_rec;
+        w.rec_stride = h->max_points;
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used], s));
         cudaError_t e = fp64 ? launch_fp64(h->dev, sc, w, kThreads, s)
                              : launch_fp32(h->dev, sc, w, variant, s);
@@ -449,6 +459,7 @@ const DevTraj* traj_device_view(const teufel_traj_set* traj, unsigned int** stat
     if (status) *status = traj->d_status;
     return &traj->dev;
 }
+int64_t traj_max_points(const teufel_traj_set* traj) { return traj->max_points; }
 }  // namespace teufel
 
 Frame identity_frame() {
@@ -537,6 +548,8 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
     teufel_traj_set* h = new (std::nothrow) teufel_traj_set();
     if (!h) return TEUFEL_ERR_NOMEM;
     h->h_seg_offsets = segs;
+    for (int m = 0; m < n_particles; m++)
+        h->max_points = std::max<int64_t>(h->max_points, n_points[m]);
     cudaGetDevice(&h->device);
     auto fail = [&](int code) {
         teufel_cuda_traj_free(h);
@@ -624,6 +637,7 @@ void teufel_cuda_default_options(teufel_options* opt) {
     opt->n_slots = 0;
     opt->kernel_variant = 0;
     opt->timing = 0;
+    opt->max_device_mib = 0;
 }
 
 const char* teufel_cuda_status_string(int status) {
@@ -802,6 +816,13 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     }
     if (!finite_array(pix_pos, 3 * (int64_t)Np) || !finite_array(pix_t0, Np)) return TEUFEL_ERR_ARG;
     const size_t nout = (size_t)Np * (size_t)Nt * 6;
+    // the staged pixel and trace buffers count against the caller's bound
+    const size_t staged = sizeof(double) * (4 * (size_t)Np + nout);
+    if (opt.max_device_mib > 0) {
+        const bool fp64 = opt.precision == TEUFEL_PREC_FP64 || dt < 0.0 || h->dev.non_monotone;
+        const size_t slot = nout * (fp64 ? sizeof(double) : sizeof(float));
+        if (((size_t)opt.max_device_mib << 20) < staged + slot) return TEUFEL_ERR_NOMEM;
+    }
     if ((rc = grow((void**)&h->d_pix, &h->pix_cap, sizeof(double) * 4 * (size_t)Np, false))) return rc;
     if ((rc = grow((void**)&h->d_out, &h->out_cap, sizeof(double) * nout, false))) return rc;
     double* d_pos = h->d_pix;
@@ -823,7 +844,7 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
                              h->copy_s));
     TRY_CUDA(cudaEventRecord(h->cev[1], h->copy_s));
     const HostOut ho{out, h->copy_s, h->cev[1], h->cev.data() + 3, kOutChunks};
-    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s, 100, &ho);
+    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s, 100, &ho, nullptr, staged);
     if (rc) {
         cudaStreamSynchronize(h->copy_s);
         cudaStreamSynchronize(s);
@@ -1045,6 +1066,59 @@ int teufel_cuda_point_decisions(const teufel_traj_set* traj, int m, const double
     cudaFree(d_u);
     cudaFree(d_band);
     return e ? cuda_fail(e) : TEUFEL_OK;
+}
+
+int teufel_cuda_record_decisions(const teufel_traj_set* traj_c, const double* pix_pos,
+                                 const double* pix_t0, double dt, int Nt, int Np,
+                                 const teufel_options* opt_in, int32_t* rec, double* out) {
+    teufel_traj_set* h = const_cast<teufel_traj_set*>(traj_c);
+    if (!rec || !valid_screen_args(h, pix_pos, pix_t0, dt, Nt, Np, out)) return TEUFEL_ERR_ARG;
+    teufel_options opt;
+    teufel_cuda_default_options(&opt);
+    if (opt_in) opt = *opt_in;
+    opt.device_pointers = 0;
+    opt.timing = 0;
+    if (opt.precision != TEUFEL_PREC_FP32_SPLIT) return TEUFEL_ERR_ARG;
+    // the kernels the automatic choice runs: variant 4 (default) and 8
+    if (opt.kernel_variant == 0) opt.kernel_variant = 4;
+    if (opt.kernel_variant != 4 && opt.kernel_variant != 8) return TEUFEL_ERR_ARG;
+    const size_t n_rec = (size_t)std::max(Np, 0) * (size_t)h->dev.n_particles *
+                         (size_t)h->max_points;
+    if (n_rec) std::memset(rec, 0, sizeof(int32_t) * n_rec);
+    for (auto& c : h->last_counters) c = 0;
+    if (Nt < 2 || Np == 0 || h->dev.n_particles == 0 || h->dev.n_segments == 0) return TEUFEL_OK;
+    // the FP32 kernels need dt > 0 and increasing arrivals
+    if (!(dt > 0.0) || h->dev.non_monotone) return TEUFEL_ERR_ARG;
+    if (!finite_array(pix_pos, 3 * (int64_t)Np) || !finite_array(pix_t0, Np)) return TEUFEL_ERR_ARG;
+    const size_t nout = (size_t)Np * (size_t)Nt * 6;
+    double* d_pix = nullptr;
+    double* d_out = nullptr;
+    int* d_rec = nullptr;
+    auto cleanup = [&](int rc) {
+        cudaDeviceSynchronize();
+        if (d_pix) cudaFree(d_pix);
+        if (d_out) cudaFree(d_out);
+        if (d_rec) cudaFree(d_rec);
+        return rc;
+    };
+    if (cudaMalloc(&d_pix, sizeof(double) * 4 * (size_t)Np) != cudaSuccess ||
+        cudaMalloc(&d_out, sizeof(double) * nout) != cudaSuccess ||
+        cudaMalloc(&d_rec, sizeof(int) * std::max<size_t>(n_rec, 1)) != cudaSuccess)
+        return cleanup(cuda_fail(cudaErrorMemoryAllocation));
+    if (cudaMemcpy(d_pix, pix_pos, sizeof(double) * 3 * Np, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(d_pix + 3 * (size_t)Np, pix_t0, sizeof(double) * Np, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(d_out, out, sizeof(double) * nout, cudaMemcpyHostToDevice) ||
+        cudaMemset(d_rec, 0, sizeof(int) * std::max<size_t>(n_rec, 1)))
+        return cleanup(cuda_fail(cudaGetLastError()));
+    cudaStream_t s = nullptr;
+    int rc = run_device(h, d_pix, d_pix + 3 * (size_t)Np, dt, Nt, Np, d_out, opt, s, 100, nullptr,
+                        d_rec);
+    if (rc) return cleanup(rc);
+    rc = finish(h, s);
+    if (cudaMemcpy(out, d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost) ||
+        (n_rec && cudaMemcpy(rec, d_rec, sizeof(int) * n_rec, cudaMemcpyDeviceToHost)))
+        return cleanup(cuda_fail(cudaGetLastError()));
+    return cleanup(rc);
 }
 
 int teufel_cuda_deposit_injected(int n_particles, const int* n_points, const double* ts,

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <numeric>
 #include <vector>
@@ -35,6 +36,18 @@ struct teufel_batch {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     bool ran = false;
+    // what a recorded run (teufel_cuda_batch_record_decisions) launches again
+    const DevTraj* d_tr = nullptr;
+    const DevScreen* d_sc = nullptr;
+    DevWork* d_wk = nullptr;
+    const BatchItem* d_items = nullptr;
+    double* const* d_out = nullptr;
+    const int64_t* d_prefix = nullptr;
+    int n_planned = 0;
+    int64_t n_bins = 0;
+    std::vector<DevWork> h_wk;
+    std::vector<int> plan_of_obs;    // planned index of each observer, -1 without work
+    std::vector<int64_t> rec_size;   // per planned observer: Np * particles * max points
 };
 
 namespace {
@@ -203,6 +216,14 @@ int teufel_cuda_batch_create(int n_obs, const teufel_observer* obs, const teufel
         return plans[x.obs].item_cost > plans[y.obs].item_cost;
     });
     b->n_items = (int)items.size();
+    b->plan_of_obs.assign(n_obs, -1);
+    for (int k = 0; k < np_; k++) {
+        b->plan_of_obs[plans[k].obs] = k;
+        b->rec_size.push_back((int64_t)obs[plans[k].obs].Np * trv[plans[k].obs]->n_particles *
+                              traj_max_points(obs[plans[k].obs].traj));
+        h_wk[k].rec = nullptr;
+        h_wk[k].rec_stride = traj_max_points(obs[plans[k].obs].traj);
+    }
     DevTraj* d_tr = nullptr;
     DevScreen* d_sc = nullptr;
     DevWork* d_wk = nullptr;
@@ -224,6 +245,16 @@ int teufel_cuda_batch_create(int n_obs, const teufel_observer* obs, const teufel
                                       cudaMemcpyHostToDevice)) ||
         cudaMemset(d_scratch, 0, std::max<size_t>((size_t)scratch_total, 1)))
         return fail(fail_cuda(cudaGetLastError()));
+
+    b->d_tr = d_tr;
+    b->d_sc = d_sc;
+    b->d_wk = d_wk;
+    b->d_items = d_items;
+    b->d_out = d_out;
+    b->d_prefix = d_prefix;
+    b->n_planned = np_;
+    b->n_bins = h_prefix[np_];
+    b->h_wk = h_wk;
 
     // ---- the graph: reset the queue and status, integrate, reduce ----
     for (cudaEvent_t& e : b->ev)
@@ -281,6 +312,43 @@ int teufel_cuda_batch_status(teufel_batch* b, int64_t* work_items, int64_t* inwi
     }
     if (inwindow) *inwindow = (int64_t)cnt[0];
     if (kernel_ms) *kernel_ms = ms;
+    if (mask & (1u << TEUFEL_ERR_ARG)) return TEUFEL_ERR_ARG;
+    if (mask & (1u << TEUFEL_ERR_RANGE)) return TEUFEL_ERR_RANGE;
+    return mask ? TEUFEL_ERR_CUDA : TEUFEL_OK;
+}
+
+int teufel_cuda_batch_record_decisions(teufel_batch* b, int obs, int32_t* rec) {
+    if (!b || !rec || obs < 0 || obs >= (int)b->plan_of_obs.size()) return TEUFEL_ERR_ARG;
+    const int k = b->plan_of_obs[obs];
+    if (k < 0) return TEUFEL_OK;  // an observer without work records nothing
+    const size_t n_rec = (size_t)b->rec_size[k];
+    std::memset(rec, 0, sizeof(int32_t) * n_rec);
+    int* d_rec = nullptr;
+    cudaError_t e = cudaMalloc(&d_rec, sizeof(int) * std::max<size_t>(n_rec, 1));
+    if (e) return fail_cuda(e);
+    std::vector<DevWork> wk = b->h_wk;
+    wk[k].rec = d_rec;
+    cudaStream_t s = b->cap;
+    e = cudaMemsetAsync(d_rec, 0, sizeof(int) * std::max<size_t>(n_rec, 1), s);
+    if (!e) e = cudaMemcpyAsync(b->d_wk, wk.data(), sizeof(DevWork) * wk.size(),
+                                cudaMemcpyHostToDevice, s);
+    if (!e) e = cudaMemsetAsync(b->d_head, 0, sizeof(unsigned int), s);
+    if (!e) e = cudaMemsetAsync(b->d_status, 0, sizeof(unsigned int), s);
+    if (!e && b->n_items > 0)
+        e = launch_fp32_pair_batch(b->d_tr, b->d_sc, b->d_wk, b->d_items, b->n_items, b->d_head,
+                                   std::min(b->n_blocks, b->n_items), s, true);
+    if (!e && b->n_bins > 0)
+        e = launch_reduce_fp32_batch(b->d_wk, b->d_sc, b->d_out, b->d_prefix, b->n_planned,
+                                     b->n_bins, s);
+    // the graph's own work descriptors back in place
+    if (!e) e = cudaMemcpyAsync(b->d_wk, b->h_wk.data(), sizeof(DevWork) * b->h_wk.size(),
+                                cudaMemcpyHostToDevice, s);
+    unsigned int mask = 0;
+    if (!e) e = cudaMemcpyAsync(&mask, b->d_status, sizeof(mask), cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    if (!e && n_rec) e = cudaMemcpy(rec, d_rec, sizeof(int) * n_rec, cudaMemcpyDeviceToHost);
+    cudaFree(d_rec);
+    if (e) return fail_cuda(e);
     if (mask & (1u << TEUFEL_ERR_ARG)) return TEUFEL_ERR_ARG;
     if (mask & (1u << TEUFEL_ERR_RANGE)) return TEUFEL_ERR_RANGE;
     return mask ? TEUFEL_ERR_CUDA : TEUFEL_OK;

@@ -15,7 +15,8 @@
 // Operations are written in the reference's evaluation order and the file is
 // compiled with -ffp-contract=off, so on one machine the trajectories are
 // bit-identical to the ones the reference's own pusher produces (checked in
-// tests/test_trajgen.py against fixtures made by the compiled reference).
+// tests/test_oracle_pusher.py and tests/test_oracle_vs_ref.py against fixtures
+// made by the compiled reference).
 //
 // The bunch sampler (splitmix64 + Box-Muller) is this project's own: the
 // reference seeds from std::random_device (src/bunch.cpp:40-41), which is not
