@@ -11,10 +11,23 @@
 // set is uploaded, so every operand pair comes straight out of shared memory.
 // Bin decisions, fallbacks and the sink stay per particle.
 //
-// Both particles deposit into the lane's one pixel row; each keeps its own
-// open bin.  A bin that both happen to hold open is added to twice by the
-// fire-and-forget reductions, which is the sum the trace needs.
+// The step loop has one warp vote per step.  When every lane's steps are
+// regular (both points resolved without the exact fallback, inside the trace,
+// advancing by 0 or 1 bin) or certainly outside the window, the warp deposits
+// them on a straight-line path without branches; anything else -- a point
+// within its error bound of a bin edge, a step at the window's edge or one
+// that spans several bins -- takes the general path, which is the reference's
+// full case analysis (src/particle.cpp:786-865).
+//
+// Each particle's open bin is implicit: the register accumulator of a
+// particle always holds the not-yet-added contribution to the bin of its
+// current point (B + k).  A step that leaves that bin adds the accumulator
+// to the partial trace with fire-and-forget reductions and starts the next
+// bin, so no bin index is carried or compared.  Both particles deposit into
+// the lane's one pixel row.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "lw_fp32_point.cuh"
 
@@ -25,37 +38,55 @@ namespace teufel {
 // ---------------------------------------------------------------------------
 // A pair-point is kPairPoint float4, the two particles interleaved component
 // by component (lo/hi halves: particle a, b):
-//   0-1  e (offset from the segment's first point), dt of the step it starts
+//   0-1  e (offset from the segment's first point), dt of the step that ends here
 //   2-3  beta^, 1 - |beta|
 //   4-5  scaled beta', velocity-field scale
-//   6-7  dA = beta^_i - c^_i, 1 - |beta_c|   (c^_i: chord of the step i -> i+1)
-//   8-9  dB = beta^_(i+1) - c^_i, unused
-// all in the set's frame.  dA and dB give the arrival-increment shares
-// 1 - c^.N = (1 - beta^.N) + d.N of the step's two end points from the field's
-// own 1 - beta^.N; they are formed in FP64, so their FP32 values carry full
-// relative precision however small they are.
-// dA, dB of point k of a particle with points [o, o + n), in the set's frame
-__device__ __forceinline__ void chord_offsets(const DevTraj& tr, int64_t o, int64_t n, int64_t k,
-                                              double3& dA, double3& dB) {
-    auto bhat = [&](int64_t q) {
-        const double4_32a bg = tr.pp[q];
-        const double P = sqrt(bg.x * bg.x + bg.y * bg.y + bg.z * bg.z);
-        return P > 0.0 ? make_double3(bg.x / P, bg.y / P, bg.z / P) : make_double3(0.0, 0.0, 1.0);
-    };
-    double3 c = make_double3(0.0, 0.0, 1.0);
-    const double3 b1 = bhat(k);
-    double3 b2 = b1;
-    if (k + 1 < o + n) {
-        const double4_32a p = tr.tx[k], q = tr.tx[k + 1];
-        const double ex = q.y - p.y, ey = q.z - p.z, ez = q.w - p.w;
-        const double L = sqrt(ex * ex + ey * ey + ez * ez);
-        if (L > 0.0) c = make_double3(ex / L, ey / L, ez / L);
-        b2 = bhat(k + 1);
-    } else {
-        c = b1;  // no step starts at the last point
+//   6-7  dA = beta^_i - c^_i, 1 - |beta_c| of the step that ends here
+//   8-9  dB = beta^_i - c^_(i-1), unused
+// all in the set's frame (c^_i: chord direction of the step i -> i+1).  dA and
+// dB give the arrival-increment shares 1 - c^.N = (1 - beta^.N) + d.N of the
+// point for the step that starts (dA) and the step that ends (dB) there, from
+// the field's own 1 - beta^.N; they are formed in FP64, so their FP32 values
+// carry full relative precision however small they are.  Everything the step
+// ending at point i needs beyond the state of point i-1 lives in pair-point i.
+__device__ __forceinline__ double3 unit_bg(const DevTraj& tr, int64_t q) {
+    const double4_32a bg = tr.pp[q];
+    const double P = sqrt(bg.x * bg.x + bg.y * bg.y + bg.z * bg.z);
+    return P > 0.0 ? make_double3(bg.x / P, bg.y / P, bg.z / P) : make_double3(0.0, 0.0, 1.0);
+}
+// chord direction of the step q -> q+1 (the velocity direction where the step
+// has no length)
+__device__ __forceinline__ double3 chord_dir(const DevTraj& tr, int64_t q) {
+    const double4_32a p = tr.tx[q], r = tr.tx[q + 1];
+    const double ex = r.y - p.y, ey = r.z - p.z, ez = r.w - p.w;
+    const double L = sqrt(ex * ex + ey * ey + ez * ez);
+    return L > 0.0 ? make_double3(ex / L, ey / L, ez / L) : unit_bg(tr, q);
+}
+
+// The per-point data of point k (local index l) of a particle with points
+// [o, o + n); beyond its last point (l >= n) the last point is repeated with
+// a step of zero duration ending at it.
+__device__ __forceinline__ void pair_point_data(const DevTraj& tr, int64_t o, int64_t n, int64_t l,
+                                                float4& q0, float4& q1, float4& q2, float& dtp,
+                                                float& cepsp, double3& dA, double3& dB) {
+    const int64_t k = o + (l < n ? l : n - 1);
+    q0 = tr.q0[k];
+    q1 = tr.q1[k];
+    q2 = tr.q2[k];
+    const double3 b = unit_bg(tr, k);
+    // the step starting here (none at the last point)
+    const double3 cA = k + 1 < o + n ? chord_dir(tr, k) : b;
+    dA = make_double3(b.x - cA.x, b.y - cA.y, b.z - cA.z);
+    dtp = 0.0f;
+    cepsp = 1.0f;
+    dB = make_double3(0.0, 0.0, 0.0);
+    if (l >= 1 && l < n) {
+        // the step ending here: its duration, 1 - |chord velocity| and chord
+        dtp = tr.q0[k - 1].w;
+        cepsp = tr.q3[k - 1].w;
+        const double3 cB = chord_dir(tr, k - 1);
+        dB = make_double3(b.x - cB.x, b.y - cB.y, b.z - cB.z);
     }
-    dA = make_double3(b1.x - c.x, b1.y - c.y, b1.z - c.z);
-    dB = make_double3(b2.x - c.x, b2.y - c.y, b2.z - c.z);
     to_frame(tr.frame, dA.x, dA.y, dA.z);
     to_frame(tr.frame, dB.x, dB.y, dB.z);
 }
@@ -74,33 +105,31 @@ __global__ void prep_pairs_kernel(DevTraj tr, float4* pq) {
     const int ma = 2 * j, mb = 2 * j + 1 < tr.n_particles ? 2 * j + 1 : 2 * j;
     const int64_t oa = tr.offsets[ma], na = tr.offsets[ma + 1] - oa;
     const int64_t ob = tr.offsets[mb], nb = tr.offsets[mb + 1] - ob;
-    float4 a0, a1, a2, a3, b0, b1, b2, b3;
+    float4 a0, a1, a2, b0, b1, b2;
+    float dta = 0.0f, cea = 1.0f, dtb = 0.0f, ceb = 1.0f;
     double3 dAa = make_double3(0.0, 0.0, 0.0), dBa = dAa, dAb = dAa, dBb = dAa;
     if (na > 0) {
-        const int64_t k = oa + (l < na ? l : na - 1);
-        a0 = tr.q0[k]; a1 = tr.q1[k]; a2 = tr.q2[k]; a3 = tr.q3[k];
-        chord_offsets(tr, oa, na, k, dAa, dBa);
+        pair_point_data(tr, oa, na, l, a0, a1, a2, dta, cea, dAa, dBa);
     } else {
-        a0 = a1 = a2 = a3 = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
+        a0 = a1 = a2 = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
     }
     if (nb > 0) {
-        const int64_t k = ob + (l < nb ? l : nb - 1);
-        b0 = tr.q0[k]; b1 = tr.q1[k]; b2 = tr.q2[k]; b3 = tr.q3[k];
-        chord_offsets(tr, ob, nb, k, dAb, dBb);
+        pair_point_data(tr, ob, nb, l, b0, b1, b2, dtb, ceb, dAb, dBb);
     } else {
-        b0 = a0; b1 = a1; b2 = a2; b3 = a3;
+        b0 = a0; b1 = a1; b2 = a2;
+        dtb = dta; ceb = cea;
         dAb = dAa;
         dBb = dBa;
     }
     float4* o = pq + kPairPoint * i;
     o[0] = make_float4(a0.x, b0.x, a0.y, b0.y);
-    o[1] = make_float4(a0.z, b0.z, a0.w, b0.w);
+    o[1] = make_float4(a0.z, b0.z, dta, dtb);
     o[2] = make_float4(a1.x, b1.x, a1.y, b1.y);
     o[3] = make_float4(a1.z, b1.z, a1.w, b1.w);
     o[4] = make_float4(a2.x, b2.x, a2.y, b2.y);
     o[5] = make_float4(a2.z, b2.z, a2.w, b2.w);
     o[6] = make_float4((float)dAa.x, (float)dAb.x, (float)dAa.y, (float)dAb.y);
-    o[7] = make_float4((float)dAa.z, (float)dAb.z, a3.w, b3.w);
+    o[7] = make_float4((float)dAa.z, (float)dAb.z, cea, ceb);
     o[8] = make_float4((float)dBa.x, (float)dBb.x, (float)dBa.y, (float)dBb.y);
     o[9] = make_float4((float)dBa.z, (float)dBb.z, 0.0f, 0.0f);
 }
@@ -126,10 +155,22 @@ __device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2{add2(a.v, b.v)};
 __device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2{sub2(a.v, b.v)}; }
 __device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2{mul2(a.v, b.v)}; }
 __device__ __forceinline__ F2 fma(F2 a, F2 b, F2 c) { return F2{fma2(a.v, b.v, c.v)}; }
-__device__ __forceinline__ F2 rsqrt2(F2 a) { return f2(rsqrtf(a.v.x), rsqrtf(a.v.y)); }
-__device__ __forceinline__ F2 rcp2(F2 a) {
-    return f2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y));
+// The hardware approximations without the denormal handling of rsqrtf() and
+// __fdividef(): no operand of these is ever subnormal (squared distances,
+// 1 + beta^.N, kappa, sums of 1/R, step lengths in bins), and for normal
+// operands the results are the same.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ F2 rsqrt2(F2 a) { return f2(rsqrt_ftz(a.v.x), rsqrt_ftz(a.v.y)); }
+__device__ __forceinline__ F2 rcp2(F2 a) { return f2(rcp_ftz(a.v.x), rcp_ftz(a.v.y)); }
 struct V2 {
     F2 x, y, z;
 };
@@ -154,12 +195,11 @@ struct PairPoint {
 __device__ __forceinline__ F2 lo2(float4 v) { return f2(v.x, v.y); }
 __device__ __forceinline__ F2 hi2(float4 v) { return f2(v.z, v.w); }
 
+// The state of one point of a pair as the walk carries it.
 struct PointState2 {
-    int ka, kb;     // ki of particles a, b
-    F2 r;
-    int idxa, idxb; // bin indices (general path only)
-    int fla, flb;   // window flags; kExact when resolved exactly, else 0 until materialized
-    bool rega, regb;  // resolved without fallback, bin inside the trace
+    int ka, kb;     // B + ka is the bin of particle a's point (likewise b)
+    int exa, exb;   // 0, or rec_encode(bin, flags) of a point resolved exactly
+    F2 r;           // the rest of (ts - t0)/dt - B - k, in [-1/2, 1/2] normally
     F2 iR;          // 1/|R|
     F2 aplus;       // 1 - c^.N with c^ the chord of the step this point starts
     F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
@@ -183,11 +223,10 @@ __device__ __forceinline__ Anchor2 pack_anchor(const Anchor& a, const Anchor& b)
 }
 
 // point_field (lw_fp32_point.cuh) for both particles at once, plus the point's
-// shares of the arrival increments (step_increment2): 1 - c^.N for the chord
-// of the step that ends here (from qprev's dB, returned in aminus) and of the
-// step that starts here (from q's dA, kept in S.aplus), as 1 - beta^.N + d.N.
-__device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
-                                             const PairPoint& qprev, const Anchor2& A,
+// shares of the arrival increments: 1 - c^.N for the chord of the step that
+// ends here (from dB, returned in aminus) and of the step that starts here
+// (from dA, kept in S.aplus), as 1 - beta^.N + d.N.
+__device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q, const Anchor2& A,
                                              F2& aminus) {
     const V2 e{lo2(q.d[0]), hi2(q.d[0]), lo2(q.d[1])};
     const V2 b{lo2(q.d[2]), hi2(q.d[2]), lo2(q.d[3])};
@@ -204,7 +243,7 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
     const F2 a0 = dot(W, W) * rc1;  // 1 - beta^.N
     const F2 kappa = fma(one - eps, a0, eps);
     S.aplus = a0 + dot(V2{lo2(q.d[6]), hi2(q.d[6]), lo2(q.d[7])}, N);
-    aminus = a0 + dot(V2{lo2(qprev.d[8]), hi2(qprev.d[8]), lo2(qprev.d[9])}, N);
+    aminus = a0 + dot(V2{lo2(q.d[8]), hi2(q.d[8]), lo2(q.d[9])}, N);
     const V2 Sv = N + b;
     const V2 T = cross(W, Sv);
     const V2 mb{fma(T.x, rc1, b.x * eps), fma(T.y, rc1, b.y * eps), fma(T.z, rc1, b.z * eps)};
@@ -225,8 +264,8 @@ __device__ __forceinline__ void point_field2(PointState2& S, const PairPoint& q,
 // The arrival increment of the step from point 1 to point 2 [bins] for both
 // particles: step_increment (lw_fp32_point.cuh) with the points' shares
 // 1 - c^.N formed when each point was evaluated (point_field2), so a point
-// state carries two numbers instead of N.  q is the pair-point the step
-// starts at (its chord and dt).
+// state carries two numbers instead of N.  q is the pair-point the step ends
+// at (its duration and chord 1 - |beta_c|).
 __device__ __forceinline__ F2 step_increment2(const PointState2& p1, const PointState2& p2,
                                               F2 aminus, const PairPoint& q, F2 kdt) {
     const F2 ceps = hi2(q.d[7]);
@@ -237,17 +276,23 @@ __device__ __forceinline__ F2 step_increment2(const PointState2& p1, const Point
     return dt * kdt * kap;
 }
 
+// Advance the compensated chain from p1 to p2 by du >= 0.  The integer part
+// is split off by adding and subtracting 1.5 * 2^23, which rounds to the
+// nearest integer (ties to even, as rintf) for |t| < 2^22; the integer is the
+// low bits of t + 1.5 * 2^23.  Larger or non-finite t cannot pass the
+// fallback test, whose bound grows with du: the point is then re-evaluated
+// exactly.
+constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
 __device__ __forceinline__ void chain_step2(const PointState2& p1, PointState2& p2, F2 du,
                                             F2& comp) {
     const F2 y = du - comp;
-    F2 t = p1.r + y;
+    const F2 t = p1.r + y;
     comp = (t - p1.r) - y;
-    const float tx = fminf(fmaxf(t.v.x, -4.0e8f), 4.0e8f);
-    const float ty = fminf(fmaxf(t.v.y, -4.0e8f), 4.0e8f);
-    const float kx = rintf(tx), ky = rintf(ty);
-    p2.r = f2(tx, ty) - f2(kx, ky);
-    p2.ka = p1.ka + (int)kx;
-    p2.kb = p1.kb + (int)ky;
+    const F2 m = t + f2(kRoundMagic, kRoundMagic);
+    const F2 k = m - f2(kRoundMagic, kRoundMagic);
+    p2.r = t - k;
+    p2.ka = p1.ka + (__float_as_int(m.v.x) - __float_as_int(kRoundMagic));
+    p2.kb = p1.kb + (__float_as_int(m.v.y) - __float_as_int(kRoundMagic));
 }
 
 __device__ __forceinline__ void start_chain2(PointState2& S, const Anchor2& A) {
@@ -257,14 +302,22 @@ __device__ __forceinline__ void start_chain2(PointState2& S, const Anchor2& A) {
     S.r = A.frac - f2(kx, ky);
 }
 
-// One particle of a pair as a PointState, for the general deposit.
+// One particle of a pair as a PointState for the general deposit, with its
+// bin index and window flags: those of the exact evaluation where the point
+// was resolved exactly, else those its bin implies.
 template <int W>
-__device__ __forceinline__ PointState unpack(const PointState2& S) {
+__device__ __forceinline__ PointState unpack(const PointState2& S, int B, int nt) {
     PointState p;
     p.ki = W ? S.kb : S.ka;
     p.r = W ? S.r.v.y : S.r.v.x;
-    p.idx = W ? S.idxb : S.idxa;
-    p.flags = W ? S.flb : S.fla;
+    const int ex = W ? S.exb : S.exa;
+    if (ex) {
+        p.idx = (ex & ((1 << kRecFlagShift) - 1)) - 4;
+        p.flags = ex >> kRecFlagShift;
+    } else {
+        p.flags = 0;
+        materialize(p, B, nt);
+    }
 #pragma unroll
     for (int c = 0; c < 3; c++)
         p.f[c] = W ? make_float2(S.f[2 * c].v.y, S.f[2 * c + 1].v.y)
@@ -286,25 +339,12 @@ __device__ __forceinline__ void red_add6_if(bool p, float* addr, float a0, float
         : "memory");
 }
 
-// ---------------------------------------------------------------------------
-// The sink of a lane: one pixel row, an open bin per particle, accumulators
-// in packed form (component c of particles a and b).  Closed bins are added
-// with fire-and-forget reductions, as RedSink (lw_fp32_point.cuh) does.
-// ---------------------------------------------------------------------------
-struct PairSink {
+// The register accumulators of a lane: component c of particles a and b.
+// acc holds, for each particle, what its current point's bin has received
+// and not yet added to the partial trace (the pixel's row).
+struct PairAcc {
     F2 acc[6];
-    int open_a, open_b;
     float* row;
-    unsigned int err;
-    unsigned int n_add;
-    __device__ void init(float* r) {
-        row = r;
-        open_a = open_b = -1;
-        err = 0;
-        n_add = 0;
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = f2(0.0f, 0.0f);
-    }
     template <int W>
     __device__ __forceinline__ float get(int c) const {
         return W ? acc[c].v.y : acc[c].v.x;
@@ -314,196 +354,87 @@ struct PairSink {
         if (W) acc[c].v.y = v; else acc[c].v.x = v;
     }
     template <int W>
-    __device__ __forceinline__ void reduce_to(int k) {
-        float2* p = reinterpret_cast<float2*>(row + (int64_t)k * 6);
-        atomicAdd(p, make_float2(get<W>(0), get<W>(1)));
-        atomicAdd(p + 1, make_float2(get<W>(2), get<W>(3)));
-        atomicAdd(p + 2, make_float2(get<W>(4), get<W>(5)));
-    }
-    template <int W>
-    __device__ __forceinline__ void flush() {
-        int& open = W ? open_b : open_a;
-        if (open < 0) return;
-        reduce_to<W>(open);
-        open = -1;
-    }
-    // The RedSink contract for particle W: f = component pairs (Ex,Ey),
-    // (Ez,cBx), (cBy,cBz).
-    template <int W>
-    __device__ __forceinline__ void add(int k, const float2* f, int nt) {
-        if (k < 0 || k >= nt) {
-            err |= 1u << TEUFEL_ERR_RANGE;
-            return;
-        }
-        n_add++;
-        int& open = W ? open_b : open_a;
-        if (k == open) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                set<W>(2 * c, get<W>(2 * c) + f[c].x);
-                set<W>(2 * c + 1, get<W>(2 * c + 1) + f[c].y);
-            }
-        } else {
-            flush<W>();
-            open = k;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                set<W>(2 * c, f[c].x);
-                set<W>(2 * c + 1, f[c].y);
-            }
-        }
-    }
-    // Regular steps of both particles: fa/fb say which particle deposits
-    // (its weights are zero otherwise), ka/kb its bin, sa/sb whether the step
-    // crosses into bin k+1.  Bin k receives f1 a1 + f2 b1, bin k+1 (on a
-    // crossing) f1 a2 + f2 b2, fused into the accumulators.
-    __device__ __forceinline__ void add_fast(bool fa, bool fb, int ka, int kb, bool sa, bool sb,
-                                             const F2* f1, const F2* f2v, F2 a1, F2 b1, F2 a2,
-                                             F2 b2) {
-        // a bin other than the open one: only after a general-path step or at
-        // the start of a walk, so one branch for both particles
-        const bool na = fa && ka != open_a, nb = fb && kb != open_b;
-        if (na || nb) {
-            if (na) {
-                flush<0>();
-                open_a = ka;
-#pragma unroll
-                for (int c = 0; c < 6; c++) acc[c].v.x = 0.0f;
-            }
-            if (nb) {
-                flush<1>();
-                open_b = kb;
-#pragma unroll
-                for (int c = 0; c < 6; c++) acc[c].v.y = 0.0f;
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = fma(f2v[c], b1, fma(f1[c], a1, acc[c]));
-        // a step that crosses into the next bin closes its bin: predicated
-        // reductions, no divergent branch
-        reduce_if<0>(sa, ka);
-        reduce_if<1>(sb, kb);
-        open_a = sa ? ka + 1 : open_a;
-        open_b = sb ? kb + 1 : open_b;
-        const F2 keep = f2(sa ? 0.0f : 1.0f, sb ? 0.0f : 1.0f);
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, fma(f2v[c], b2, f1[c] * a2));
-        n_add += (unsigned)fa + (unsigned)fb + (unsigned)sa + (unsigned)sb;
-    }
-    // Regular steps of both particles that may span several bins: ka/kb the
-    // first bin, spa/spb >= 0 the bins spanned beyond it (0 for a particle
-    // that does not deposit).  The first bin receives f1 a1 + f2 b1 and closes
-    // when the step spans; each full bin k1 + j, 0 < j < span, receives
-    // f1 w1(j) + f2 w2(j) with w1(j) = (u2 - j) rd, w2(j) = (j - u1) rd in bin
-    // units from k1 (u1 = r1, u2 = span + r2); the last bin opens with
-    // f1 a2 + f2 b2.
-    __device__ __forceinline__ void add_multi(bool fa, bool fb, int ka, int kb, int spa, int spb,
-                                              const F2* f1, const F2* f2v, F2 a1, F2 b1, F2 a2,
-                                              F2 b2, F2 u1, F2 u2, F2 rd) {
-        const bool na = fa && ka != open_a, nb = fb && kb != open_b;
-        if (na || nb) {
-            if (na) {
-                flush<0>();
-                open_a = ka;
-#pragma unroll
-                for (int c = 0; c < 6; c++) acc[c].v.x = 0.0f;
-            }
-            if (nb) {
-                flush<1>();
-                open_b = kb;
-#pragma unroll
-                for (int c = 0; c < 6; c++) acc[c].v.y = 0.0f;
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = fma(f2v[c], b1, fma(f1[c], a1, acc[c]));
-        const bool sa = spa > 0, sb = spb > 0;
-        reduce_if<0>(sa, ka);
-        reduce_if<1>(sb, kb);
-        // full bins, in bin order per particle
-        const int nfull = max(spa, spb) - 1;
-        for (int j = 1; j <= nfull; j++) {
-            const F2 jj = f2((float)j, (float)j);
-            const F2 w1 = (u2 - jj) * rd, w2 = (jj - u1) * rd;
-            F2 g[6];
-#pragma unroll
-            for (int c = 0; c < 6; c++) g[c] = fma(f2v[c], w2, f1[c] * w1);
-            const bool pa = j < spa, pb = j < spb;
-            float* qa = row + (int64_t)(ka + j) * 6;
-            float* qb = row + (int64_t)(kb + j) * 6;
-            red_add6_if(pa, qa, g[0].v.x, g[1].v.x, g[2].v.x, g[3].v.x, g[4].v.x, g[5].v.x);
-            red_add6_if(pb, qb, g[0].v.y, g[1].v.y, g[2].v.y, g[3].v.y, g[4].v.y, g[5].v.y);
-        }
-        open_a = sa ? ka + spa : open_a;
-        open_b = sb ? kb + spb : open_b;
-        const F2 keep = f2(sa ? 0.0f : 1.0f, sb ? 0.0f : 1.0f);
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[c] = fma(acc[c], keep, fma(f2v[c], b2, f1[c] * a2));
-        n_add += (unsigned)fa + (unsigned)fb + (unsigned)spa + (unsigned)spb;
-    }
-    template <int W>
     __device__ __forceinline__ void reduce_if(bool p, int k) {
         red_add6_if(p, row + (int64_t)k * 6, get<W>(0), get<W>(1), get<W>(2), get<W>(3),
                     get<W>(4), get<W>(5));
     }
+    template <int W>
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int c = 0; c < 6; c++) set<W>(c, 0.0f);
+    }
 };
 
-// The decision taken for point i of particle m (particle W of the pair) at
-// this lane's pixel: the exact evaluation's bin and flags where the point
-// fell back to it, else the bin B + ki and the window flags it implies (as
-// materialize does), into the decision record.  A point evaluated twice (the
-// last point of one slot is the first of the next) must get the same
-// decision both times; a difference is flagged.
+// The general deposit's sink for particle W: the reference's bin
+// contributions in increasing bin order, merged in the accumulator while
+// they go to one bin; `open` is the accumulator's bin (-1: none).
 template <int W>
-__device__ __forceinline__ void record_point(const DevWork& wk, int n_particles, int pix, int m,
-                                             int i, const PointState2& q, int B, int nt) {
-    const int f = W ? q.flb : q.fla;
-    int idx, fl;
-    if (f & kExact) {
-        idx = W ? q.idxb : q.idxa;
-        fl = f;
-    } else {
-        int k = B + (W ? q.kb : q.ka);
-        k = k < -2 ? -2 : (k > nt + 1 ? nt + 1 : k);
-        idx = k;
-        fl = (k < 0 ? kLeTmin : 0) | (k < nt ? kLtTmax : 0);
-    }
-    const int v = rec_encode(idx, fl);
-    int* p = wk.rec + ((int64_t)pix * n_particles + m) * wk.rec_stride + i;
-    const int old = atomicCAS(p, 0, v);
-    if (old != 0 && old != v) atomicOr(p, kRecConflict);
-}
-
-template <int W>
-struct PairView {
-    PairSink* s;
+struct GeneralSink {
+    PairAcc* a;
+    int open;
     int nt;
-    __device__ __forceinline__ void add(int k, const float2* f) { s->add<W>(k, f, nt); }
+    unsigned int* err;
+    unsigned int* n_add;
+    __device__ __forceinline__ void add(int k, const float2* f) {
+        if (k < 0 || k >= nt) {
+            *err |= 1u << TEUFEL_ERR_RANGE;
+            return;
+        }
+        (*n_add)++;
+        if (k == open) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                a->template set<W>(2 * c, a->template get<W>(2 * c) + f[c].x);
+                a->template set<W>(2 * c + 1, a->template get<W>(2 * c + 1) + f[c].y);
+            }
+        } else {
+            a->template reduce_if<W>(open >= 0, open);
+            open = k;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                a->template set<W>(2 * c, f[c].x);
+                a->template set<W>(2 * c + 1, f[c].y);
+            }
+        }
+    }
 };
 
 // Regular steps of both particles (deposit_fast, lw_fp32_point.cuh, in packed
-// form).  fa/fb: the particle deposits a regular step.  The step's trapezoid
-// (fields f1, f2 at arrival r1 < r2 [bins]) is split at the bin edge when it
-// crosses one: with dts = r2 - r1 (+1 on a crossing), a the part in bin k
-// (dts when no crossing), lam = a/dts and fe = (1 - lam) f1 + lam f2,
+// form).  da/db: the particle deposits a regular step (k2 - k1 in {0, 1});
+// ca/cb: its point leaves the bin of the step's start (for a particle that
+// does not deposit, by any number of bins).  The step's trapezoid (fields f1,
+// f2 at arrival r1 < r2 [bins]) is split at the bin edge when it crosses
+// one: with dts = r2 - r1 (+1 on a crossing), a the part in bin k (dts when
+// no crossing), lam = a/dts and fe = (1 - lam) f1 + lam f2,
 //   bin k:   (f1 + fe) a/2       = f1 (2 - lam) a/2       + f2 lam a/2,
 //   bin k+1: (fe + f2) (dts-a)/2 = f1 (1 - lam) (dts-a)/2 + f2 (1 + lam) (dts-a)/2.
+// Bin k's part goes into the accumulator; on a crossing the accumulator is
+// added to bin k (k1a/k1b: B + k of the step's start, v1a/v1b: inside the
+// trace) and restarts with bin k+1's part.
 __device__ __forceinline__ void deposit_fast2(const PointState2& p1, const PointState2& p2,
-                                              int Ba, int Bb, bool fa, bool fb, PairSink& sink) {
-    const bool sa = fa && p2.ka != p1.ka, sb = fb && p2.kb != p1.kb;
-    const F2 dts = f2(sa ? 1.0f : 0.0f, sb ? 1.0f : 0.0f) + (p2.r - p1.r);
+                                              bool da, bool db, bool ca, bool cb, int k1a,
+                                              int k1b, bool v1a, bool v1b, PairAcc& s) {
+    const F2 dts = f2(ca ? 1.0f : 0.0f, cb ? 1.0f : 0.0f) + (p2.r - p1.r);
     const F2 h = f2(0.5f, 0.5f) - p1.r;
-    const F2 a = f2(sa ? h.v.x : dts.v.x, sb ? h.v.y : dts.v.y);
-    // lam = 1 without a crossing: dts may be zero there (a particle past its
-    // last point repeats it)
+    const F2 a = f2(ca ? h.v.x : dts.v.x, cb ? h.v.y : dts.v.y);
     const F2 q = a * rcp2(dts);
-    const F2 lam = f2(sa ? q.v.x : 1.0f, sb ? q.v.y : 1.0f);
-    const F2 hw1 = f2(fa ? 0.5f * a.v.x : 0.0f, fb ? 0.5f * a.v.y : 0.0f);
-    const F2 hw2 = f2(0.5f, 0.5f) * (dts - a);  // zero without a crossing
+    // lam = 1 without a crossing or a deposit (dts may be zero there: a
+    // particle past its last point repeats it)
+    const F2 lam = f2(ca && da ? q.v.x : 1.0f, cb && db ? q.v.y : 1.0f);
+    const F2 hw1 = f2(da ? 0.5f * a.v.x : 0.0f, db ? 0.5f * a.v.y : 0.0f);
+    const F2 t2 = f2(0.5f, 0.5f) * (dts - a);  // zero without a crossing
+    const F2 hw2 = f2(da ? t2.v.x : 0.0f, db ? t2.v.y : 0.0f);
     const F2 one = f2(1.0f, 1.0f);
     const F2 a1 = (f2(2.0f, 2.0f) - lam) * hw1, b1 = lam * hw1;
     const F2 a2 = (one - lam) * hw2, b2 = (one + lam) * hw2;
-    sink.add_fast(fa, fb, Ba + p1.ka, Bb + p1.kb, sa, sb, p1.f, p2.f, a1, b1, a2, b2);
+#pragma unroll
+    for (int c = 0; c < 6; c++) s.acc[c] = fma(p2.f[c], b1, fma(p1.f[c], a1, s.acc[c]));
+    // predicated reductions, no divergent branch
+    s.reduce_if<0>(ca && v1a, k1a);
+    s.reduce_if<1>(cb && v1b, k1b);
+    const F2 keep = f2(ca ? 0.0f : 1.0f, cb ? 0.0f : 1.0f);
+#pragma unroll
+    for (int c = 0; c < 6; c++) s.acc[c] = fma(s.acc[c], keep, fma(p2.f[c], b2, p1.f[c] * a2));
 }
 
 // Regular steps that span several bins (deposit_step32's first partial, full
@@ -516,7 +447,7 @@ __device__ __forceinline__ void multi_weights(bool f, int sp, float r1, float r2
                                               float& b1, float& a2, float& b2, float& u2,
                                               float& rd) {
     const float dts = (float)sp + (r2 - r1);
-    rd = __fdividef(1.0f, dts);
+    rd = rcp_ftz(dts);
     u2 = (float)sp + r2;
     // first bin: from u1 to its upper edge; last bin: from its lower edge to u2
     const float h1 = 0.5f - r1, h2 = (float)sp - 0.5f + r2;
@@ -530,14 +461,63 @@ __device__ __forceinline__ void multi_weights(bool f, int sp, float r1, float r2
     b2 = f && spans ? s2b : 0.0f;
 }
 
+// The multi-bin form of deposit_fast2: spa/spb >= 0 the bins a depositing
+// particle's step spans beyond its first (0 for one that does not deposit).
+// The first bin receives f1 a1 + f2 b1 and is added when the point leaves it;
+// each full bin k1 + j, 0 < j < span, receives f1 w1(j) + f2 w2(j) with
+// w1(j) = (u2 - j) rd, w2(j) = (j - u1) rd in bin units from k1 (u1 = r1,
+// u2 = span + r2); the last bin starts with f1 a2 + f2 b2.
 __device__ __forceinline__ void deposit_multi2(const PointState2& p1, const PointState2& p2,
-                                               int Ba, int Bb, bool fa, bool fb, PairSink& sink) {
-    const int spa = fa ? p2.ka - p1.ka : 0, spb = fb ? p2.kb - p1.kb : 0;
+                                               bool da, bool db, bool ca, bool cb, int k1a,
+                                               int k1b, bool v1a, bool v1b, PairAcc& s) {
+    const int spa = da ? p2.ka - p1.ka : 0, spb = db ? p2.kb - p1.kb : 0;
     float a1x, b1x, a2x, b2x, u2x, rdx, a1y, b1y, a2y, b2y, u2y, rdy;
-    multi_weights(fa, spa, p1.r.v.x, p2.r.v.x, a1x, b1x, a2x, b2x, u2x, rdx);
-    multi_weights(fb, spb, p1.r.v.y, p2.r.v.y, a1y, b1y, a2y, b2y, u2y, rdy);
-    sink.add_multi(fa, fb, Ba + p1.ka, Bb + p1.kb, spa, spb, p1.f, p2.f, f2(a1x, a1y), f2(b1x, b1y),
-                   f2(a2x, a2y), f2(b2x, b2y), p1.r, f2(u2x, u2y), f2(rdx, rdy));
+    multi_weights(da, spa, p1.r.v.x, p2.r.v.x, a1x, b1x, a2x, b2x, u2x, rdx);
+    multi_weights(db, spb, p1.r.v.y, p2.r.v.y, a1y, b1y, a2y, b2y, u2y, rdy);
+    const F2 a1 = f2(a1x, a1y), b1 = f2(b1x, b1y), a2 = f2(a2x, a2y), b2 = f2(b2x, b2y);
+    const F2 u1 = p1.r, u2 = f2(u2x, u2y), rd = f2(rdx, rdy);
+#pragma unroll
+    for (int c = 0; c < 6; c++) s.acc[c] = fma(p2.f[c], b1, fma(p1.f[c], a1, s.acc[c]));
+    s.reduce_if<0>(ca && v1a, k1a);
+    s.reduce_if<1>(cb && v1b, k1b);
+    // full bins, in bin order per particle
+    const int nfull = max(spa, spb) - 1;
+    for (int j = 1; j <= nfull; j++) {
+        const F2 jj = f2((float)j, (float)j);
+        const F2 w1 = (u2 - jj) * rd, w2 = (jj - u1) * rd;
+        F2 g[6];
+#pragma unroll
+        for (int c = 0; c < 6; c++) g[c] = fma(p2.f[c], w2, p1.f[c] * w1);
+        const bool pa = j < spa, pb = j < spb;
+        red_add6_if(pa, s.row + (int64_t)(k1a + j) * 6, g[0].v.x, g[1].v.x, g[2].v.x, g[3].v.x,
+                    g[4].v.x, g[5].v.x);
+        red_add6_if(pb, s.row + (int64_t)(k1b + j) * 6, g[0].v.y, g[1].v.y, g[2].v.y, g[3].v.y,
+                    g[4].v.y, g[5].v.y);
+    }
+    const F2 keep = f2(ca ? 0.0f : 1.0f, cb ? 0.0f : 1.0f);
+#pragma unroll
+    for (int c = 0; c < 6; c++) s.acc[c] = fma(s.acc[c], keep, fma(p2.f[c], b2, p1.f[c] * a2));
+}
+
+// The decision taken for point i of particle m (particle W of the pair) at
+// this lane's pixel: the exact evaluation's bin and flags where the point
+// fell back to it, else the bin B + k and the window flags it implies (as
+// materialize does), into the decision record.  A point evaluated twice (the
+// last point of one slot is the first of the next) must get the same
+// decision both times; a difference is flagged.
+template <int W>
+__device__ __forceinline__ void record_point(const DevWork& wk, int n_particles, int pix, int m,
+                                             int i, const PointState2& q, int B, int nt) {
+    const int ex = W ? q.exb : q.exa;
+    int v = ex;
+    if (!ex) {
+        int k = B + (W ? q.kb : q.ka);
+        k = k < -2 ? -2 : (k > nt + 1 ? nt + 1 : k);
+        v = rec_encode(k, (k < 0 ? kLeTmin : 0) | (k < nt ? kLtTmax : 0));
+    }
+    int* p = wk.rec + ((int64_t)pix * n_particles + m) * wk.rec_stride + i;
+    const int old = atomicCAS(p, 0, v);
+    if (old != 0 && old != v) atomicOr(p, kRecConflict);
 }
 
 // ---------------------------------------------------------------------------
@@ -553,24 +533,22 @@ constexpr int kPChunkShift = 4;
 constexpr int kPChunkLen = 1 << kPChunkShift;
 static_assert(kSegLen % kPChunkLen == 0 && kPChunkLen % 2 == 0, "chunk layout");
 
-// A staged chunk: p[0] is the pair-point before the chunk (the start of the
-// chunk's first step), p[1 + l] the chunk's point l.
+// A staged chunk: p[l] is the chunk's point l.
 struct __align__(16) PairChunk {
-    PairPoint p[kPChunkLen + 1];
+    PairPoint p[kPChunkLen];
 };
 
-// The 32 lanes copy pair-points p0-1 .. p0+avail-1 of the pair whose data
-// starts at pq (p[0] only when p0 > 0).
+// The 32 lanes copy pair-points p0 .. p0+avail-1 of the pair whose data
+// starts at pq.
 __device__ __forceinline__ void pair_stage(PairChunk* b, const float4* pq, int p0, int avail,
                                            int lane) {
-    const int skip = p0 > 0 ? 0 : kPairPoint;  // float4s of p[0] not copied
-    const int n = kPairPoint * (avail + 1);
-    const float4* src = pq + kPairPoint * ((int64_t)p0 - 1);
+    const int n = kPairPoint * avail;
+    const float4* src = pq + kPairPoint * (int64_t)p0;
     float4* dst = reinterpret_cast<float4*>(b->p);
 #pragma unroll
-    for (int k = 0; k < (kPairPoint * (kPChunkLen + 1) + 31) / 32; k++) {
+    for (int k = 0; k < (kPairPoint * kPChunkLen + 31) / 32; k++) {
         const int t = lane + 32 * k;
-        if (t >= skip && t < n) {
+        if (t < n) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + t);
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + t)
                          : "memory");
@@ -641,11 +619,15 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                                     sc.pix_t0[pc], sc.dt, sc.nt);
     if (lane == 0) sh.stats[0] = sh.stats[1] = 0;
     const PixelCtx& px = sh.px[threadIdx.x];
+    const int nt = sc.nt;
+    // bins this lane may add to: none for a lane without a pixel
+    const unsigned nt_lane = active ? (unsigned)nt : 0u;
     PairChunk* wb = sh.buf;
     PairWalk& W = sh.walk;
-    PairSink sink;
-    sink.init(static_cast<float*>(wk.scratch) + (int64_t)slot * wk.slot_stride +
-              (int64_t)pc * sc.nt * 6);
+    PairAcc s;
+    s.row = static_cast<float*>(wk.scratch) + (int64_t)slot * wk.slot_stride +
+            (int64_t)pc * nt * 6;
+    unsigned int err = 0, n_add = 0;
     const int64_t g0 = wk.slot_seg[slot], g1 = wk.slot_seg[slot + 1];
     int j = g0 < g1 ? pair_of_segment(tr.pair_seg_offsets, tr.n_pairs, g0) : tr.n_pairs;
     // a slot holds at most 2048 particles of at most 2^31 points: the
@@ -687,10 +669,126 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         }
         __syncwarp();
         pair_stage(&wb[0], W.pq, start, min(kPChunkLen, W.npp - start), lane);
-        Anchor2 A;
+        Anchor2 A{};  // made at the walk's first chunk
         PointState2 p1, p2;
         F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);  // chain_err includes A.err
-        p2.rega = p2.regb = false;
+
+        // The point is close enough to a bin edge that the estimate cannot
+        // decide it (NaN-safe: a non-finite estimate falls back as well).
+        auto near = [&](const PointState2& q) {
+            const bool na = !(0.5f - fabsf(q.r.v.x) > chain_err.v.x);
+            const bool nb = !(0.5f - fabsf(q.r.v.y) > chain_err.v.y);
+            return make_int2(na, nb);
+        };
+        // the exact evaluation of point i of particle w
+        auto resolve = [&](PointState2& q, int w, int i) {
+            if (w == 0) {
+                const ExactPoint e = exact_point(W.txa, i, px, A.Ba);
+                q.ka = e.ki;
+                q.r.v.x = e.r;
+                q.exa = rec_encode(e.idx, e.flags);
+            } else {
+                const ExactPoint e = exact_point(W.txb, i, px, A.Bb);
+                q.kb = e.ki;
+                q.r.v.y = e.r;
+                q.exb = rec_encode(e.idx, e.flags);
+            }
+            atomicAdd(&sh.stats[1], 1ull);
+        };
+
+        // One step: point l of the chunk into q2 (the chain continued from q1,
+        // or started afresh at a new anchor), then the step q1 -> q2 deposited.
+        auto step = [&](auto fresh, PointState2& q1, PointState2& q2, const PairChunk& B, int l,
+                        int i) {
+            F2 aminus;
+            point_field2(q2, B.p[l], A, aminus);
+            q2.exa = q2.exb = 0;
+            if constexpr (decltype(fresh)::value) {
+                start_chain2(q2, A);
+                comp = f2(0.0f, 0.0f);
+                chain_err = A.err;
+            } else {
+                const F2 du = step_increment2(q1, q2, aminus, B.p[l], f2(px.kdt, px.kdt));
+                chain_step2(q1, q2, du, comp);
+                // du >= 0: arrivals increase along the points
+                chain_err = fma(du, f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));
+            }
+            // the step ending at point i belongs to this lane and slot
+            const bool dep_a = i <= lim_a, dep_b = i <= lim_b;
+            const int2 nr = near(q2);
+            const int k1a = A.Ba + q1.ka, k1b = A.Bb + q1.kb;
+            const int k2a = A.Ba + q2.ka, k2b = A.Bb + q2.kb;
+            // regular: resolved without the fallback, bin inside the trace
+            const bool r1a = q1.exa == 0 && (unsigned)k1a < (unsigned)nt;
+            const bool r1b = q1.exb == 0 && (unsigned)k1b < (unsigned)nt;
+            const bool r2a = !nr.x && (unsigned)k2a < (unsigned)nt;
+            const bool r2b = !nr.y && (unsigned)k2b < (unsigned)nt;
+            const bool fast_a = r1a && r2a && (unsigned)(q2.ka - q1.ka) <= 1u;
+            const bool fast_b = r1b && r2b && (unsigned)(q2.kb - q1.kb) <= 1u;
+            // certainly outside the window: adds nothing
+            const bool out_a = (!nr.x && k2a < 0) || (q1.exa == 0 && k1a >= nt);
+            const bool out_b = (!nr.y && k2b < 0) || (q1.exb == 0 && k1b >= nt);
+            const bool ok_a = !dep_a || (!nr.x && (fast_a || out_a));
+            const bool ok_b = !dep_b || (!nr.y && (fast_b || out_b));
+            const bool ca = q2.ka != q1.ka, cb = q2.kb != q1.kb;
+            const bool v1a = (unsigned)k1a < nt_lane, v1b = (unsigned)k1b < nt_lane;
+            bool go_multi = false;
+            bool multi_a = false, multi_b = false;
+            const bool go_fast = __all_sync(0xffffffffu, ok_a && ok_b);
+            if constexpr (MULTI) {
+                multi_a = r1a && r2a && (unsigned)(q2.ka - q1.ka) <= (unsigned)kMaxSpan;
+                multi_b = r1b && r2b && (unsigned)(q2.kb - q1.kb) <= (unsigned)kMaxSpan;
+                if (!go_fast)
+                    go_multi = __all_sync(0xffffffffu,
+                                          (!dep_a || (!nr.x && (multi_a || out_a))) &&
+                                              (!dep_b || (!nr.y && (multi_b || out_b))));
+            }
+            if (go_fast) {
+                const bool da = dep_a && fast_a, db = dep_b && fast_b;
+                deposit_fast2(q1, q2, da, db, ca, cb, k1a, k1b, v1a, v1b, s);
+                inwin += (unsigned)da + (unsigned)db;
+                n_add += (unsigned)da + (unsigned)db + (unsigned)(da && ca) + (unsigned)(db && cb);
+            } else if (go_multi) {
+                const bool da = dep_a && multi_a, db = dep_b && multi_b;
+                deposit_multi2(q1, q2, da, db, ca, cb, k1a, k1b, v1a, v1b, s);
+                inwin += (unsigned)da + (unsigned)db;
+                n_add += (unsigned)da + (unsigned)db + (unsigned)(da ? q2.ka - q1.ka : 0) +
+                         (unsigned)(db ? q2.kb - q1.kb : 0);
+            } else {
+                // the general path: exact fallbacks, then the reference's
+                // deposit per particle through the accumulator of its bin
+                if (dep_a && nr.x) resolve(q2, 0, i);
+                if (dep_b && nr.y) resolve(q2, 1, i);
+                {
+                    GeneralSink<0> g{&s, v1a ? k1a : -1, nt, &err, &n_add};
+                    if (dep_a) {
+                        const PointState u1 = unpack<0>(q1, A.Ba, nt), u2 = unpack<0>(q2, A.Ba, nt);
+                        if (deposit_step32(u1, u2, A.Ba, nt, g)) inwin++;
+                    }
+                    // the accumulator belongs to the bin of the new point
+                    const bool moved = g.open != A.Ba + q2.ka;
+                    s.reduce_if<0>(moved && g.open >= 0, g.open);
+                    if (moved) s.clear<0>();
+                }
+                {
+                    GeneralSink<1> g{&s, v1b ? k1b : -1, nt, &err, &n_add};
+                    if (dep_b) {
+                        const PointState u1 = unpack<1>(q1, A.Bb, nt), u2 = unpack<1>(q2, A.Bb, nt);
+                        if (deposit_step32(u1, u2, A.Bb, nt, g)) inwin++;
+                    }
+                    const bool moved = g.open != A.Bb + q2.kb;
+                    s.reduce_if<1>(moved && g.open >= 0, g.open);
+                    if (moved) s.clear<1>();
+                }
+            }
+            if constexpr (REC) {
+                if (dep_a) record_point<0>(wk, tr.n_particles, pix, ma, i, q2, A.Ba, nt);
+                if (dep_b) record_point<1>(wk, tr.n_particles, pix, mb, i, q2, A.Bb, nt);
+            }
+        };
+
+        const std::integral_constant<bool, true> kFresh;
+        const std::integral_constant<bool, false> kChained;
         const int n_chunks = (W.n_pts + kPChunkLen - 1) >> kPChunkShift;
         for (int c = 0; c < n_chunks; c++) {
             const int p0 = start + (c << kPChunkShift);
@@ -719,137 +817,71 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 if (wa <= 0) aa = ab;
                 const Anchor2 An = pack_anchor(aa, ab);
                 if (c > 0) {
-                    // rebase the chunk's previous point (in p2, see below):
-                    // B + ki is unchanged
-                    p2.ka += A.Ba - An.Ba;
-                    p2.kb += A.Bb - An.Bb;
+                    // rebase the previous point: B + k is unchanged
+                    p1.ka += A.Ba - An.Ba;
+                    p1.kb += A.Bb - An.Bb;
                 }
                 A = An;
             }
             const int n_here = min(kPChunkLen, W.n_pts - (c << kPChunkShift));
-            // One step: point l of the chunk into q2, deposit q1 -> q2.  The
-            // loop below alternates the roles of p1 and p2, so the point
-            // state is never copied.
-            auto step = [&](PointState2& q1, PointState2& q2, int l) {
-                const int i = p0 + l;
+            int l = 0;
+            if (c == 0) {
+                // the walk's first point: no step ends there
                 F2 aminus;
-                point_field2(q2, B.p[l + 1], B.p[l], A, aminus);
-                if (l == 0 && anchor) {
-                    start_chain2(q2, A);
-                    comp = f2(0.0f, 0.0f);
-                    chain_err = A.err;
-                } else {
-                    const F2 du = step_increment2(q1, q2, aminus, B.p[l], f2(px.kdt, px.kdt));
-                    chain_step2(q1, q2, du, comp);
-                    chain_err = fma(f2(fabsf(du.v.x), fabsf(du.v.y)),
-                                    f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));
-                }
-                // the step ending at point i belongs to this lane and slot
-                const bool dep_a = i > start && i <= lim_a;
-                const bool dep_b = i > start && i <= lim_b;
-                const int nt = sc.nt;
-                const bool near_a = 0.5f - fabsf(q2.r.v.x) <= chain_err.v.x && i <= lim_a;
-                const bool near_b = 0.5f - fabsf(q2.r.v.y) <= chain_err.v.y && i <= lim_b;
-                q2.fla = 0;
-                q2.flb = 0;
-                q2.rega = !near_a && (unsigned)(A.Ba + q2.ka) < (unsigned)nt;
-                q2.regb = !near_b && (unsigned)(A.Bb + q2.kb) < (unsigned)nt;
-                if (near_a || near_b) {  // rare: one branch for both particles
-                    if (near_a) {
-                        const ExactPoint e = exact_point(W.txa, i, px, A.Ba);
-                        q2.ka = e.ki;
-                        q2.r.v.x = e.r;
-                        q2.idxa = e.idx;
-                        q2.fla = e.flags;
-                        atomicAdd(&sh.stats[1], 1ull);
-                    }
-                    if (near_b) {
-                        const ExactPoint e = exact_point(W.txb, i, px, A.Bb);
-                        q2.kb = e.ki;
-                        q2.r.v.y = e.r;
-                        q2.idxb = e.idx;
-                        q2.flb = e.flags;
-                        atomicAdd(&sh.stats[1], 1ull);
-                    }
-                }
+                point_field2(p1, B.p[0], A, aminus);
+                p1.exa = p1.exb = 0;
+                start_chain2(p1, A);
+                comp = f2(0.0f, 0.0f);
+                chain_err = A.err;
+                const int2 nr = near(p1);
+                if (nr.x && start <= lim_a) resolve(p1, 0, start);
+                if (nr.y && start <= lim_b) resolve(p1, 1, start);
                 if constexpr (REC) {
-                    if (i <= lim_a) record_point<0>(wk, tr.n_particles, pix, ma, i, q2, A.Ba, nt);
-                    if (i <= lim_b) record_point<1>(wk, tr.n_particles, pix, mb, i, q2, A.Bb, nt);
+                    if (start <= lim_a)
+                        record_point<0>(wk, tr.n_particles, pix, ma, start, p1, A.Ba, nt);
+                    if (start <= lim_b)
+                        record_point<1>(wk, tr.n_particles, pix, mb, start, p1, A.Bb, nt);
                 }
-                const bool fast_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= 1u;
-                const bool fast_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= 1u;
-                bool go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a) && (!dep_b || fast_b));
-                bool out_a = false, out_b = false;
-                if (!go_fast) {
-                    // steps that certainly lie outside the window add nothing
-                    // and leave the fast path open
-                    out_a = (q2.fla == 0 && A.Ba + q2.ka < 0) ||
-                            (!(q1.fla & kExact) && A.Ba + q1.ka >= nt);
-                    out_b = (q2.flb == 0 && A.Bb + q2.kb < 0) ||
-                            (!(q1.flb & kExact) && A.Bb + q1.kb >= nt);
-                    go_fast = __all_sync(0xffffffffu, (!dep_a || fast_a || out_a) &&
-                                                          (!dep_b || fast_b || out_b));
-                }
-                // regular steps that span up to kMaxSpan bins beyond their first
-                bool multi_a = false, multi_b = false, go_multi = false;
-                if constexpr (MULTI) {
-                    multi_a = q1.rega && q2.rega && (unsigned)(q2.ka - q1.ka) <= (unsigned)kMaxSpan;
-                    multi_b = q1.regb && q2.regb && (unsigned)(q2.kb - q1.kb) <= (unsigned)kMaxSpan;
-                    if (!go_fast)
-                        go_multi = __all_sync(0xffffffffu, (!dep_a || multi_a || out_a) &&
-                                                               (!dep_b || multi_b || out_b));
-                }
-                if (go_fast) {
-                    const bool da = dep_a && fast_a, db = dep_b && fast_b;
-                    // unconditional: a particle without a deposit adds zeros (its
-                    // fields are finite for any observer off its trajectory)
-                    deposit_fast2(q1, q2, A.Ba, A.Bb, da, db, sink);
-                    inwin += (unsigned)da + (unsigned)db;
-                } else if (go_multi) {
-                    const bool da = dep_a && multi_a, db = dep_b && multi_b;
-                    deposit_multi2(q1, q2, A.Ba, A.Bb, da, db, sink);
-                    inwin += (unsigned)da + (unsigned)db;
-                } else {
-                    if (dep_a) {
-                        PointState u1 = unpack<0>(q1), u2 = unpack<0>(q2);
-                        materialize(u1, A.Ba, nt);
-                        materialize(u2, A.Ba, nt);
-                        PairView<0> v{&sink, nt};
-                        if (deposit_step32(u1, u2, A.Ba, nt, v)) inwin++;
-                    }
-                    if (dep_b) {
-                        PointState u1 = unpack<1>(q1), u2 = unpack<1>(q2);
-                        materialize(u1, A.Bb, nt);
-                        materialize(u2, A.Bb, nt);
-                        PairView<1> v{&sink, nt};
-                        if (deposit_step32(u1, u2, A.Bb, nt, v)) inwin++;
-                    }
-                }
-            };
+#pragma unroll
+                for (int q = 0; q < 6; q++) s.acc[q] = f2(0.0f, 0.0f);
+                l = 1;
+            } else if (anchor) {
+                step(kFresh, p1, p2, B, 0, p0);
+                p1 = p2;
+                l = 1;
+            }
             if (PINGPONG) {
-                // chunks are kPChunkLen (even) points long, so point l of every
-                // chunk lives in p1 for even l and in p2 for odd l, and the
-                // point before a chunk in p2
-                for (int l = 0; l < n_here; l += 2) {
-                    step(p2, p1, l);
-                    if (l + 1 < n_here) step(p1, p2, l + 1);
+                // two steps per trip with the roles of the point states
+                // alternating: no copy of the state
+                for (; l + 1 < n_here; l += 2) {
+                    step(kChained, p1, p2, B, l, p0 + l);
+                    step(kChained, p2, p1, B, l + 1, p0 + l + 1);
+                }
+                if (l < n_here) {
+                    step(kChained, p1, p2, B, l, p0 + l);
+                    p1 = p2;
                 }
             } else {
                 // one copy of the step body (fewer registers), the new point
                 // copied into place after each step
-                for (int l = 0; l < n_here; l++) {
-                    step(p2, p1, l);
-                    p2 = p1;
+                for (; l < n_here; l++) {
+                    step(kChained, p1, p2, B, l, p0 + l);
+                    p1 = p2;
                 }
             }
             __syncwarp();  // the buffer is restaged two chunks later
         }
+        // what the accumulators still hold belongs to the bins of the walk's
+        // last point
+        {
+            const int ka = A.Ba + p1.ka, kb = A.Bb + p1.kb;
+            s.reduce_if<0>((unsigned)ka < nt_lane, ka);
+            s.reduce_if<1>((unsigned)kb < nt_lane, kb);
+        }
     }
-    sink.flush<0>();
-    sink.flush<1>();
-    if (sink.err) atomicOr(wk.status, sink.err);
+    if (err) atomicOr(wk.status, err);
     const unsigned long long win = warp_sum_u64(inwin);
-    const unsigned long long nadd = warp_sum_u64(sink.n_add);
+    const unsigned long long nadd = warp_sum_u64(n_add);
     __syncwarp();
     if (lane == 0 && wk.counters) {
         if (win) atomicAdd(wk.counters, win);
@@ -861,12 +893,11 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 
 // MAXREG: the register budget per thread, which sets how many one-warp
 // blocks are resident per SM (65536 / (32 MAXREG)): 128 -> 16, 136 -> 15,
-// 144 -> 14, 160 -> 13 (the unrolled loop needs ~152).  PINGPONG: the inner
-// loop unrolled by two with alternating point states (no copies, more
-// registers) or one step body with a copy per step.  MULTI: warps whose
-// regular steps span up to kMaxSpan bins deposit them on packed pairs too
-// (instead of per particle); for observers whose bins are short against the
-// arrival advance of a step.  It costs ~1% where steps rarely span.
+// 144 -> 14, 160 -> 13.  PINGPONG: the inner loop unrolled by two with
+// alternating point states (no copies, more registers) or one step body with
+// a copy per step.  MULTI: warps whose regular steps span up to kMaxSpan bins
+// deposit them on packed pairs too (instead of per particle); for observers
+// whose bins are short against the arrival advance of a step.
 //
 // REC: the recording instantiation, which also writes every point decision it
 // takes into DevWork::rec (the parity tests compare them with the oracle's);
