@@ -325,18 +325,19 @@ __device__ __forceinline__ PointState unpack(const PointState2& S, int B, int nt
     return p;
 }
 
-// The six components of one bin, added by three red.global.add.v2.f32 under
-// one predicate: the L2 adds them when p holds.  One asm block, so the
-// predicate is formed once and the addresses are immediate offsets.
+// The six components of one bin, added by three red.global.add.v2.f32 when p
+// holds: the L2 adds them.  The reductions are issued under one branch rather
+// than each under its own predicate, which the compiler would turn into three
+// convergence regions.
 __device__ __forceinline__ void red_add6_if(bool p, float* addr, float a0, float a1, float a2,
                                             float a3, float a4, float a5) {
-    asm volatile(
-        "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %0, 0;\n\t"
-        "@q red.global.add.v2.f32 [%1], {%2, %3};\n\t"
-        "@q red.global.add.v2.f32 [%1+8], {%4, %5};\n\t"
-        "@q red.global.add.v2.f32 [%1+16], {%6, %7};\n\t}"
-        ::"r"((int)p), "l"(addr), "f"(a0), "f"(a1), "f"(a2), "f"(a3), "f"(a4), "f"(a5)
-        : "memory");
+    if (p)
+        asm volatile(
+            "red.global.add.v2.f32 [%0], {%1, %2};\n\t"
+            "red.global.add.v2.f32 [%0+8], {%3, %4};\n\t"
+            "red.global.add.v2.f32 [%0+16], {%5, %6};"
+            ::"l"(addr), "f"(a0), "f"(a1), "f"(a2), "f"(a3), "f"(a4), "f"(a5)
+            : "memory");
 }
 
 // The register accumulators of a lane: component c of particles a and b.
