@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--fp64-full", action="store_true",
                     help="instead of the bench line: FP32 split against FP64 GPU on the full "
                          "single-electron, 1e4-particle and gamma = 2000 workloads (~10 min)")
+    ap.add_argument("--full-configs", action="store_true",
+                    help="instead of the bench line: the 1e5-particle screen as ONE integration "
+                         "call (multi-pass slots) and the 16 batched screens at a quarter of "
+                         "their particle draws (~5 min, ~220 GB of device memory)")
     return ap.parse_args()
 
 
@@ -294,6 +298,60 @@ def full_comparison():
                      "peak_sample_rel_err": float(np.abs(diff).max() / np.abs(r64).max()),
                      "tracking_s": t_track}
         del r32, r64, diff
+    return out
+
+
+def full_configs():
+    """The workloads at (or near) their stated sizes through the public API:
+    the 1e5-particle coherent-emission screen integrated by ONE
+    teufel_cuda_integrate_screen call with host buffers (its 49+ FP32 slots
+    run as successive passes of the partial-trace budget), checked against
+    the FP64 GPU path on every 400th pixel; and the 16 batched uneven screens
+    at a quarter of each screen's particle draw (the full draw's trajectories
+    alone need ~630 GB) as one persistent launch."""
+    import torch
+    from teufel_gb300 import abi, harness as H
+    out = {}
+    # ---- the 1e5-particle bunch, one call ----
+    tt = time.perf_counter()
+    w = H.config4()
+    t_track = time.perf_counter() - tt
+    npts = int(w.traj.n_points[0])
+    evals = w.n_pix * w.traj.n_particles * (npts - 1)
+    with abi.TrajSet(w.traj) as ts:
+        tv = 0  # the automatic kernel choice (one tuning trial here would take minutes)
+        res = np.zeros((w.n_pix, w.nots, 6))
+        tt = time.perf_counter()
+        ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, out=res)
+        t32 = time.perf_counter() - tt
+        _, _, launches, _, _ = ts.last_timing()
+        inwin, fallbacks, st = ts.last_inwindow()
+        sub = np.arange(0, w.n_pix, 400)
+        tt = time.perf_counter()
+        r64 = ts.integrate_screen(w.pix_pos[sub], w.pix_t0[sub], w.dt, w.nots,
+                                  precision=abi.PREC_FP64)
+        t64 = time.perf_counter() - tt
+        tt = time.perf_counter()
+        r32s = ts.integrate_screen(w.pix_pos[sub], w.pix_t0[sub], w.dt, w.nots)
+        t32s = time.perf_counter() - tt
+    diff = res[sub] - r64
+    out["bunch_1e5_200x200_4096x2fs_one_call"] = {
+        "particles": w.traj.n_particles, "points_per_particle": npts, "pixels": w.n_pix,
+        "samples": w.nots, "evals": evals, "in_window_fraction": inwin / evals,
+        "fp32_kernel": KERNEL_NAMES.get(tv, "?"), "launches": launches,
+        "passes": launches // 2, "status": st, "seconds": t32,
+        "evals_per_s": evals / t32, "tracking_s": t_track,
+        "fp64_check": {"pixels": len(sub), "rel_l2_fp32_split_vs_fp64":
+                       float(np.linalg.norm(diff) / np.linalg.norm(r64)),
+                       "peak_sample_rel_err": float(np.abs(diff).max() / np.abs(r64).max()),
+                       "fp64_gpu_s": t64, "fp32_split_s_same_pixels": t32s,
+                       "speedup_fp32_split_over_fp64": t64 / t32s}}
+    del res, r64, r32s, diff, w
+    # ---- the batched uneven screens at a quarter of their draws ----
+    dev = torch.device("cuda", 0)
+    torch.cuda.empty_cache()
+    b = batch_measure(dev, reps=2, scale=4)
+    out["batched_16_screens_quarter_draw"] = b
     return out
 
 
@@ -606,6 +664,9 @@ def main():
         return run_reference(args)
     if args.fp64_full:
         print(json.dumps({"fp32_split_vs_fp64_gpu_full_workloads": full_comparison()}))
+        return 0
+    if args.full_configs:
+        print(json.dumps({"full_configs": full_configs()}))
         return 0
     return run_gb300(args)
 
