@@ -56,6 +56,12 @@ extern "C" {
 #define TEUFEL_PREC_FP32_SPLIT 0 /* FP32 fields with split-form 1-n.beta; FP64 anchors,
                                     bin indices bit-identical to the reference */
 #define TEUFEL_PREC_FP64 1       /* plain FP64 throughout, in the reference's operation order */
+#define TEUFEL_PREC_FP32_FP64TIME 2 /* FP32 split-form fields with the reference's FP64 arrival
+                                       times, bin indices and bin edges: the deposit follows
+                                       FP64's own rounding of the arrival times.  Chosen
+                                       automatically for TEUFEL_PREC_FP32_SPLIT calls (kernel
+                                       variant 0) whose bins are short against that rounding:
+                                       2^-52 max|t0| / |dt| > 1e-6 */
 
 typedef struct teufel_traj_set teufel_traj_set; /* opaque, device-resident */
 typedef void *teufel_stream_t;                   /* a cudaStream_t; NULL = default stream */
@@ -70,7 +76,8 @@ typedef struct teufel_options {
                              4/5/6/7 = warp-uniform steps, two particles per
                              thread, 16/12/15/14 resident warps per SM,
                              8 = as 4, with packed deposits of steps that
-                             span several bins (short bins)                  */
+                             span several bins (short bins), 9 = as 4, with
+                             the FP64 arrival times of TEUFEL_PREC_FP32_FP64TIME */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
     int max_device_mib;   /* upper bound on the device memory one call may take
@@ -198,7 +205,8 @@ int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int
 /* No counterpart in the reference.  Tunes the FP32 split-precision path for
  * one observer shape: times the kernel variants (warp-uniform; two particles
  * per thread at 12 to 16 resident warps per SM, and at 16 with packed
- * multi-bin deposits) at the automatic slot count,
+ * multi-bin deposits) at the automatic slot count -- or only the FP64-time
+ * kernel (9) where TEUFEL_PREC_FP32_FP64TIME's rule selects it --
  * then the fastest at half and twice as many slots, on these very inputs,
  * writing the trial traces to a scratch buffer (out-free: nothing is added
  * anywhere).  A later candidate wins only when more than 0.5% faster than the
@@ -307,7 +315,7 @@ int teufel_cuda_point_decisions(const teufel_traj_set *traj, int m, const double
 /* The decisions the shipping FP32 kernels take, recorded by their recording
  * instantiations (the same source compiled with one more store per point).
  * Runs teufel_cuda_integrate_screen_ex with host buffers on kernel variant 4
- * (the default, also for 0) or 8 (opt->kernel_variant; opt->n_slots is
+ * (the default, also for 0), 8 or 9 (opt->kernel_variant; opt->n_slots is
  * honoured; opt may be NULL) and adds the traces into out[Np][Nt][6].
  * rec[Np][n_particles][max_points] (host, max_points = the longest particle's
  * point count) receives, for every point a kernel evaluated for a pixel as

@@ -95,7 +95,7 @@ def test_config4_shipping_kernel_decisions(c4_64, variant):
     assert rel_l2(tr, oracle) < TOL_FP32
 
 
-@pytest.mark.parametrize("variant", [4, 8])
+@pytest.mark.parametrize("variant", [4, 8, 9])
 def test_config5_shipping_kernel_decisions(variant):
     """gamma = 2000, 1 as bins: steps span several bins, chains re-anchor
     every chunk and exact fallbacks are frequent."""
@@ -106,6 +106,8 @@ def test_config5_shipping_kernel_decisions(variant):
         tr_rec, rec = ts.record_decisions(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=variant)
         tr = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=variant)
     n, n_dep, fb = check_record(rec, ref)
+    # the chained kernels fall back to the exact evaluation near bin edges;
+    # the FP64-time kernel (9) evaluates every point so
     assert n >= 1_000_000 and n_dep > 0 and fb > 0
     assert np.array_equal(tr_rec, tr)
 

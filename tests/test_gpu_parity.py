@@ -217,6 +217,66 @@ def test_bunch_subset_parity(name, cfg, count, pix_step, variant):
         assert e < TOL_FP32, (name, e)
 
 
+@pytest.mark.parametrize("how", ["automatic", "explicit"])
+def test_config5_fp64_time_matches_fp64_oracle(how):
+    """1e-18 s bins 30 m from the source: FP64's rounding of the arrival
+    times is ~1e-5 bins, so the chained FP32 arrival times (more accurate than
+    FP64's) differ from the FP64 oracle by ~1.4e-5.  The FP64-time mode --
+    chosen automatically there (2^-52 |t0| / dt = 1.3e-5 > 1e-6) or asked for
+    -- takes the reference's FP64 arrival times, bins and bin edges with FP32
+    fields, and must then meet the 1e-5 bar against the FP64 oracle itself,
+    with every bin decision the reference's."""
+    w = _bunch_case(H.config5, 6, 127)
+    ref, rc = lw.integrate_screen(w.traj, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rc == 0 and np.abs(ref).max() > 0
+    prec = abi.PREC_FP32_SPLIT if how == "automatic" else abi.PREC_FP32_FP64TIME
+    with abi.TrajSet(w.traj) as ts:
+        g = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
+        inwin, _, st = ts.last_inwindow()
+        _, rec = ts.record_decisions(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=9)
+    assert st == 0 and inwin > 0
+    e = rel_l2(g, ref)
+    print(f"config5 FP64-time ({how}): split vs fp64 {e:.3e}")
+    assert e < TOL_FP32, e
+    dec = lw.screen_decisions(w.traj, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    written = rec != 0
+    mask = (1 << 29) - 1  # bin and the two window flags
+    assert written.sum() > 0
+    assert np.array_equal(rec[written] & mask, dec[written] & mask)
+
+
+def test_fp64_time_mode_on_config4():
+    """The FP64-time mode is also right where it is not needed: the
+    1e5-particle screen's traces against the oracle within 1e-5."""
+    w = _bunch_case(H.config4, 6, 613)
+    ref, rc = lw.integrate_screen(w.traj, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rc == 0
+    with abi.TrajSet(w.traj) as ts:
+        g = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots,
+                                precision=abi.PREC_FP32_FP64TIME)
+        g_auto = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rel_l2(g, ref) < TOL_FP32
+    # 2^-52 |t0| / dt = 7e-9 there: the automatic choice keeps the chained kernel
+    assert rel_l2(g_auto, ref) < TOL_FP32
+
+
+def test_pairs_are_arrival_neighbours():
+    """Particles are paired by arrival order, not by upload order: the same
+    bunch uploaded in reversed and shuffled order gives the same traces to
+    FP32 rounding (the sum over particles does not depend on the order)."""
+    w = _bunch_case(H.config2, 9, 97)
+    ref, rc = lw.integrate_screen(w.traj, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rc == 0
+    perm = np.random.default_rng(2).permutation(w.traj.n_particles)
+    tr = w.traj.subset(list(perm))
+    with abi.TrajSet(w.traj) as ts:
+        a = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=4)
+    with abi.TrajSet(tr) as ts:
+        b = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=4)
+    assert rel_l2(a, ref) < TOL_FP32 and rel_l2(b, ref) < TOL_FP32
+    assert rel_l2(a, b) < 1e-6
+
+
 def _truncated(traj, lengths):
     """The first lengths[m] points of each particle m of traj (cycling
     through its particles)."""

@@ -26,6 +26,7 @@ E_CHARGE = 1.6021766208e-19  # src/global.h:36
 
 PREC_FP32_SPLIT = 0
 PREC_FP64 = 1
+PREC_FP32_FP64TIME = 2
 
 # The functions include/teufel_cuda.h declares (checked by the tests).
 EXPORTED = [

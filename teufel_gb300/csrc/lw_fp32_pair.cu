@@ -3,7 +3,7 @@
 //
 // As the warp-uniform kernel (lw_fp32_warp.cu), each warp owns 32 pixels and
 // walks trajectory points together, staged in shared memory.  Here every lane
-// carries two particles (a pair, 2j and 2j+1) for its pixel, and all the
+// carries two particles (a pair of arrival neighbours) for its pixel, and all the
 // per-point FP32 arithmetic -- the field, the arrival increment, the
 // compensated chain and the deposit weights -- is done on packed pairs
 // (add/sub/mul/fma.rn.f32x2), one instruction for both particles.  The
@@ -102,7 +102,8 @@ __global__ void prep_pairs_kernel(DevTraj tr, float4* pq) {
     }
     const int j = lo;
     const int64_t l = i - tr.pair_offsets[j];
-    const int ma = 2 * j, mb = 2 * j + 1 < tr.n_particles ? 2 * j + 1 : 2 * j;
+    const int ma = tr.pair_members[2 * j];
+    const int mb = tr.pair_members[2 * j + 1] >= 0 ? tr.pair_members[2 * j + 1] : ma;
     const int64_t oa = tr.offsets[ma], na = tr.offsets[ma + 1] - oa;
     const int64_t ob = tr.offsets[mb], nb = tr.offsets[mb + 1] - ob;
     float4 a0, a1, a2, b0, b1, b2;
@@ -203,6 +204,10 @@ struct PointState2 {
     F2 iR;          // 1/|R|
     F2 aplus;       // 1 - c^.N with c^ the chord of the step this point starts
     F2 f[6];        // Ex, Ey, Ez, cBx, cBy, cBz
+};
+// with the FP64 arrival times of both points (the FP64-time mode)
+struct PointState2T : PointState2 {
+    double tsa, tsb;
 };
 
 // The anchors of both particles, as the loop uses them.
@@ -500,6 +505,71 @@ __device__ __forceinline__ void deposit_multi2(const PointState2& p1, const Poin
     for (int c = 0; c < 6; c++) s.acc[c] = fma(s.acc[c], keep, fma(p2.f[c], b2, p1.f[c] * a2));
 }
 
+// The reference's deposit of one step (src/particle.cpp:786-865) with the
+// step's arrival times ts1, ts2 and the bin edges and centres in FP64, formed
+// as the reference forms them (Geo64: t0 + (k +- 1/2) dt, t0 + k dt), and the
+// fields in FP32.  Every difference of two of those times is exact in FP64
+// (they lie within a few bins of each other); the weights -- such a
+// difference over dts or dt -- are taken from it in FP32.  With the times
+// bit-identical to the reference's, the deposit follows FP64's rounding of
+// the arrival times, which on 1 as bins 30 m from the source is not
+// negligible (a few 1e-6 bins per point).
+template <class Sink>
+__device__ __forceinline__ bool deposit_step_ftime(double ts1, double ts2, int idx1, int fl1,
+                                                   int idx2, int fl2, const float2* f1,
+                                                   const float2* f2, const Geo64& geo, float kdt,
+                                                   int nt, Sink& sink) {
+    if ((fl2 & kLeTmin) || !(fl1 & kLtTmax)) return false;
+    const double dts = __dsub_rn(ts2, ts1);
+    const float rdts = rcp_ftz((float)dts);
+    if (idx2 > nt) idx2 = nt;
+    float2 field[3];
+    // f at time tq: weights w1 = (ts2 - tq)/dts, w2 = (tq - ts1)/dts
+    auto interp = [&](double tq, float2* o) {
+        const float2 w1 = splat2((float)__dsub_rn(ts2, tq) * rdts);
+        const float2 w2 = splat2((float)__dsub_rn(tq, ts1) * rdts);
+#pragma unroll
+        for (int c = 0; c < 3; c++) o[c] = fma2(f1[c], w1, mul2(f2[c], w2));
+    };
+    // the last partial bin idx2: from its start to ts2
+    auto last_bin = [&]() {
+        const double tst = geo.start(idx2);
+        interp(tst, field);
+        const float2 wb = splat2(0.5f * (float)__dsub_rn(ts2, tst) * kdt);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = mul2(add2(field[c], f2[c]), wb);
+        sink.add(idx2, field);
+    };
+    if (fl1 & kLeTmin) {
+        // the step starts before the window: bins 0 .. idx2-1 fully covered
+        for (int k = 0; k < idx2; k++) {
+            interp(geo.center(k), field);
+            sink.add(k, field);
+        }
+        if (idx2 < nt) last_bin();
+    } else if (idx1 == idx2) {
+        // the step lies within one bin
+        const float2 wb = splat2(0.5f * (float)dts * kdt);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = mul2(add2(f1[c], f2[c]), wb);
+        sink.add(idx1, field);
+    } else {
+        // first partial bin: from ts1 to its end
+        const double te = geo.end(idx1);
+        interp(te, field);
+        const float2 wb = splat2(0.5f * (float)__dsub_rn(te, ts1) * kdt);
+#pragma unroll
+        for (int c = 0; c < 3; c++) field[c] = mul2(add2(f1[c], field[c]), wb);
+        sink.add(idx1, field);
+        for (int k = idx1 + 1; k < idx2; k++) {
+            interp(geo.center(k), field);
+            sink.add(k, field);
+        }
+        if (idx2 < nt) last_bin();
+    }
+    return true;
+}
+
 // The decision taken for point i of particle m (particle W of the pair) at
 // this lane's pixel: the exact evaluation's bin and flags where the point
 // fell back to it, else the bin B + k and the window flags it implies (as
@@ -606,7 +676,7 @@ struct PairShared {
 // One pixel tile (kPThreads pixels of the observer) against one slot of the
 // trajectory set: the whole work of a block of the per-observer kernel, and
 // one work item of the batched kernel.
-template <bool PINGPONG, bool MULTI, bool REC>
+template <bool PINGPONG, bool MULTI, bool REC, bool EXACT = false>
 __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
                                           const DevWork& wk, int slot, int tile,
                                           PairShared& sh) {
@@ -639,9 +709,9 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         const int64_t se = tr.pair_seg_offsets[j + 1];
         const int lg0 = (int)((g0 > sb ? g0 : sb) - sb);
         const int lg1 = (int)((g1 < se ? g1 : se) - sb);
-        const int ma = 2 * j;
-        const bool hasb = 2 * j + 1 < tr.n_particles;
-        const int mb = hasb ? 2 * j + 1 : ma;
+        const int ma = tr.pair_members[2 * j];
+        const bool hasb = tr.pair_members[2 * j + 1] >= 0;
+        const int mb = hasb ? tr.pair_members[2 * j + 1] : ma;
         const int npa = (int)(tr.offsets[ma + 1] - tr.offsets[ma]);
         const int npb = hasb ? (int)(tr.offsets[mb + 1] - tr.offsets[mb]) : 0;
         const int st_lo = lg0 << kSegShift;
@@ -671,7 +741,8 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         __syncwarp();
         pair_stage(&wb[0], W.pq, start, min(kPChunkLen, W.npp - start), lane);
         Anchor2 A{};  // made at the walk's first chunk
-        PointState2 p1, p2;
+        using PS = std::conditional_t<EXACT, PointState2T, PointState2>;
+        PS p1, p2;
         F2 comp = f2(0.0f, 0.0f), chain_err = f2(0.0f, 0.0f);  // chain_err includes A.err
 
         // The point is close enough to a bin edge that the estimate cannot
@@ -697,12 +768,66 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             atomicAdd(&sh.stats[1], 1ull);
         };
 
+        // The FP64-time mode: point i of particle w resolved with the
+        // reference's arrival time, and the step from q1 deposited on it
+        // (ka/kb then hold the bin itself, exa/exb its encoded decision).
+        auto ftime_point = [&](auto& q, int w, int i) {
+            const double ts = exact_retarded_time(w ? W.txb[i] : W.txa[i], px.P);
+            const int idx = exact_bin(ts, px.w);
+            const int ex = rec_encode(idx, exact_flags(ts, px.w));
+            if (w) {
+                q.tsb = ts;
+                q.kb = idx;
+                q.exb = ex;
+            } else {
+                q.tsa = ts;
+                q.ka = idx;
+                q.exa = ex;
+            }
+        };
+        auto ftime_step = [&](auto wtag, const auto& q1, auto& q2, int i) {
+            constexpr int Wp = decltype(wtag)::value;
+            ftime_point(q2, Wp, i);
+            const int idx1 = Wp ? q1.kb : q1.ka, idx2 = Wp ? q2.kb : q2.ka;
+            const int fl1 = (Wp ? q1.exb : q1.exa) >> kRecFlagShift;
+            const int fl2 = (Wp ? q2.exb : q2.exa) >> kRecFlagShift;
+            float2 f1[3], f2[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                f1[c] = Wp ? make_float2(q1.f[2 * c].v.y, q1.f[2 * c + 1].v.y)
+                           : make_float2(q1.f[2 * c].v.x, q1.f[2 * c + 1].v.x);
+                f2[c] = Wp ? make_float2(q2.f[2 * c].v.y, q2.f[2 * c + 1].v.y)
+                           : make_float2(q2.f[2 * c].v.x, q2.f[2 * c + 1].v.x);
+            }
+            // the accumulator belongs to the bin of q1 (when inside the trace)
+            GeneralSink<Wp> g{&s, (unsigned)idx1 < nt_lane ? idx1 : -1, nt, &err, &n_add};
+            const Geo64 geo{px.w.t0, px.w.dt};
+            if (deposit_step_ftime(Wp ? q1.tsb : q1.tsa, Wp ? q2.tsb : q2.tsa, idx1, fl1, idx2,
+                                   fl2, f1, f2, geo, px.kdt, nt, g))
+                inwin++;
+            const bool moved = g.open != idx2;
+            s.reduce_if<Wp>(moved && g.open >= 0, g.open);
+            if (moved) s.clear<Wp>();
+        };
+        const std::integral_constant<int, 0> kPa;
+        const std::integral_constant<int, 1> kPb;
+
         // One step: point l of the chunk into q2 (the chain continued from q1,
         // or started afresh at a new anchor), then the step q1 -> q2 deposited.
-        auto step = [&](auto fresh, PointState2& q1, PointState2& q2, const PairChunk& B, int l,
-                        int i) {
+        auto step = [&](auto fresh, PS& q1, PS& q2, const PairChunk& B, int l, int i) {
             F2 aminus;
             point_field2(q2, B.p[l], A, aminus);
+            if constexpr (EXACT) {
+                // FP32 fields, the reference's FP64 arrival times: the bin and
+                // flags of every point are the reference's
+                if (i <= lim_a) ftime_step(kPa, q1, q2, i);
+                if (i <= lim_b) ftime_step(kPb, q1, q2, i);
+                if constexpr (REC) {
+                    if (i <= lim_a) record_point<0>(wk, tr.n_particles, pix, ma, i, q2, 0, nt);
+                    if (i <= lim_b) record_point<1>(wk, tr.n_particles, pix, mb, i, q2, 0, nt);
+                }
+                return;
+            }
             q2.exa = q2.exb = 0;
             if constexpr (decltype(fresh)::value) {
                 start_chain2(q2, A);
@@ -817,7 +942,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 else ab = aa;
                 if (wa <= 0) aa = ab;
                 const Anchor2 An = pack_anchor(aa, ab);
-                if (c > 0) {
+                if (c > 0 && !EXACT) {
                     // rebase the previous point: B + k is unchanged
                     p1.ka += A.Ba - An.Ba;
                     p1.kb += A.Bb - An.Bb;
@@ -834,9 +959,14 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 start_chain2(p1, A);
                 comp = f2(0.0f, 0.0f);
                 chain_err = A.err;
-                const int2 nr = near(p1);
-                if (nr.x && start <= lim_a) resolve(p1, 0, start);
-                if (nr.y && start <= lim_b) resolve(p1, 1, start);
+                if constexpr (EXACT) {
+                    if (start <= lim_a) ftime_point(p1, 0, start);
+                    if (start <= lim_b) ftime_point(p1, 1, start);
+                } else {
+                    const int2 nr = near(p1);
+                    if (nr.x && start <= lim_a) resolve(p1, 0, start);
+                    if (nr.y && start <= lim_b) resolve(p1, 1, start);
+                }
                 if constexpr (REC) {
                     if (start <= lim_a)
                         record_point<0>(wk, tr.n_particles, pix, ma, start, p1, A.Ba, nt);
@@ -875,7 +1005,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         // what the accumulators still hold belongs to the bins of the walk's
         // last point
         {
-            const int ka = A.Ba + p1.ka, kb = A.Bb + p1.kb;
+            const int ka = EXACT ? p1.ka : A.Ba + p1.ka, kb = EXACT ? p1.kb : A.Bb + p1.kb;
             s.reduce_if<0>((unsigned)ka < nt_lane, ka);
             s.reduce_if<1>((unsigned)kb < nt_lane, kb);
         }
@@ -903,11 +1033,15 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 // REC: the recording instantiation, which also writes every point decision it
 // takes into DevWork::rec (the parity tests compare them with the oracle's);
 // its arithmetic and decisions are those of the instantiation without it.
-template <int MAXREG, bool PINGPONG, bool MULTI = false, bool REC = false>
+//
+// EXACT: the FP64-time mode (FP32 fields, the reference's FP64 arrival times,
+// bins and bin edges), for observers whose bins are so short that FP64's own
+// rounding of the arrival times is not negligible against them.
+template <int MAXREG, bool PINGPONG, bool MULTI = false, bool REC = false, bool EXACT = false>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
     __shared__ PairShared sh;
-    pair_tile<PINGPONG, MULTI, REC>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
+    pair_tile<PINGPONG, MULTI, REC, EXACT>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
 }
 
 // Persistent form: every block takes (observer, tile, slot) items from the
@@ -942,6 +1076,9 @@ cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWo
         // the recording instantiations of the kernels the automatic choice uses
         if (variant == kVariantPairMulti)
             lw_fp32_pair_kernel<128, false, true, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
+        else if (variant == kVariantPairTime)
+            lw_fp32_pair_kernel<128, false, false, true, true><<<grid, kPThreads, 0, s>>>(tr, sc,
+                                                                                        w);
         else if (variant == kVariantPair)
             lw_fp32_pair_kernel<128, false, false, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
         else
@@ -961,6 +1098,10 @@ cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWo
         case kVariantPairMulti:
             lw_fp32_pair_kernel<128, false, true><<<grid, kPThreads, 0, s>>>(tr, sc, w);
             break;
+        case kVariantPairTime:
+            lw_fp32_pair_kernel<128, false, false, false, true><<<grid, kPThreads, 0, s>>>(tr, sc,
+                                                                                         w);
+            break;
         default:
             lw_fp32_pair_kernel<128, false><<<grid, kPThreads, 0, s>>>(tr, sc, w);
             break;
@@ -973,9 +1114,10 @@ int pair_batch_blocks_per_sm() { return 65536 / (32 * kBatchMaxReg); }
 
 int pair_blocks_per_sm(int variant) {
     // occupancy of the kernel of each variant, asked once
-    static int cached[5] = {-1, -1, -1, -1, -1};
+    static int cached[6] = {-1, -1, -1, -1, -1, -1};
     const int k = variant == kVariantPair160 ? 1 : variant == kVariantPair136 ? 2
-                : variant == kVariantPair144 ? 3 : variant == kVariantPairMulti ? 4 : 0;
+                : variant == kVariantPair144 ? 3 : variant == kVariantPairMulti ? 4
+                : variant == kVariantPairTime ? 5 : 0;
     if (cached[k] >= 0) return cached[k];
     int n = 0;
     cudaError_t e;
@@ -995,6 +1137,10 @@ int pair_blocks_per_sm(int variant) {
         case 4:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &n, lw_fp32_pair_kernel<128, false, true>, kPThreads, 0);
+            break;
+        case 5:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &n, lw_fp32_pair_kernel<128, false, false, false, true>, kPThreads, 0);
             break;
         default:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<128, false>,

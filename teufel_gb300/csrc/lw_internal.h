@@ -56,8 +56,12 @@ struct DevTraj {
     const float4* q2;           // [Npts] A/gamma*scale/c (xyz), scale/gamma^2
     const float4* q3;           // [Npts] chord direction of the step from here (xyz),
                                 //        1 - |chord velocity|/c
-    // Particles 2j and 2j+1 form pair j (the last pair of an odd set has one
-    // particle).  A pair is as long as its longer particle; its per-point
+    // Particles pair_members[2j] and pair_members[2j+1] form pair j (-1: the
+    // pair has one particle, the last pair of an odd set).  Pairs are formed
+    // in the order of the particles' arrival (c t - n.x of the first point,
+    // n the mean direction of the first points' momenta), so that the two
+    // particles of a pair see a trace window at nearly the same trajectory
+    // steps.  A pair is as long as its longer particle; its per-point
     // data interleaves the two particles' q0..q2 and the chord offsets
     // component by component, kPairPoint float4 per pair-point, e.g.:
     //   (e.x a, e.x b, e.y a, e.y b) (e.z a, e.z b, dt a, dt b)
@@ -73,6 +77,7 @@ struct DevTraj {
     int non_monotone;
     int n_pairs;
     int64_t n_pair_segments;
+    const int* pair_members;          // [n_pairs][2]
     const int64_t* pair_offsets;      // [n_pairs+1] first pair-point of each pair
     const int64_t* pair_seg_offsets;  // [n_pairs+1] first pair-segment of each pair
     const float4* pq;                 // [pair-points][kPairPoint]
@@ -135,7 +140,11 @@ constexpr int kVariantPair136 = 5;
 constexpr int kVariantPair144 = 6;
 // 16 resident warps per SM, with the packed deposit of steps spanning several bins
 constexpr int kVariantPairMulti = 7;
-constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPairMulti; }
+// 16 resident warps per SM, FP32 fields with the reference's FP64 arrival
+// times and bin edges (where FP64's own rounding of the arrival times is not
+// negligible against the bin width)
+constexpr int kVariantPairTime = 8;
+constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPairTime; }
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,

@@ -284,6 +284,39 @@ int64_t fill_waves(const teufel_traj_set* h, int np, int variant, int64_t slots)
     return slots;
 }
 
+// FP64's rounding of an arrival time near t0, in bins: 2^-52 |t0| / |dt|.
+// Above kFp64TimeRatio the automatic FP32 choice is the FP64-time mode, whose
+// deposit follows that rounding as the reference's does (the chained FP32
+// arrival times are more accurate than FP64's, and differ from them by about
+// this much).
+constexpr double kFp64TimeRatio = 1.0e-6;
+__global__ void max_abs_kernel(const double* v, int n, unsigned long long* out) {
+    unsigned long long m = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a = fabs(v[i]);
+        // non-negative doubles order like their bit patterns
+        m = max(m, (unsigned long long)__double_as_longlong(isfinite(a) ? a : 0.0));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+// max |t0| over the pixels (device array), read back synchronously on s
+int max_abs_t0(teufel_traj_set* h, const double* d_t0, int np, cudaStream_t s, double* out) {
+    TRY_CUDA(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long), s));
+    max_abs_kernel<<<std::min(64, (np + 255) / 256), 256, 0, s>>>(d_t0, np, h->d_counters);
+    TRY_CUDA(cudaGetLastError());
+    unsigned long long bits = 0;
+    TRY_CUDA(cudaMemcpyAsync(&bits, h->d_counters, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaStreamSynchronize(s));
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    *out = v;
+    return TEUFEL_OK;
+}
+bool needs_fp64_time(double max_abs_t0, double dt) {
+    return std::ldexp(max_abs_t0, -52) > kFp64TimeRatio * std::fabs(dt);
+}
+
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
                int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
                int slot_pct = 100, const HostOut* ho = nullptr, int* d_rec = nullptr,
@@ -298,8 +331,17 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     // sets whose arrival times can fall along a particle's points (a step
     // backwards in time or not slower than light, DevTraj::non_monotone).
     const bool fp64 = opt.precision == TEUFEL_PREC_FP64 || dt < 0.0 || h->dev.non_monotone;
+    if (!fp64 && opt.precision == TEUFEL_PREC_FP32_FP64TIME) opt.kernel_variant = 9;
     if (!fp64 && opt.kernel_variant == 0) {
-        // automatic: a tuned choice for this shape class, if there is one
+        // automatic: the FP64-time mode where FP64's rounding of the arrival
+        // times is not negligible against the bins
+        double t0max = 0.0;
+        int rc = max_abs_t0(h, d_t0, np, s, &t0max);
+        if (rc) return rc;
+        if (needs_fp64_time(t0max, dt)) opt.kernel_variant = 9;
+    }
+    if (!fp64 && opt.kernel_variant == 0) {
+        // else a tuned choice for this shape class, if there is one
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tuned.find(tune_key(h, np, nt));
         if (it != g_tuned.end()) {
@@ -314,6 +356,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                         : opt.kernel_variant == 6 ? kVariantPair136
                         : opt.kernel_variant == 7 ? kVariantPair144
                         : opt.kernel_variant == 8 ? kVariantPairMulti
+                        : opt.kernel_variant == 9 ? kVariantPairTime
                                                   : kVariantPair;  // 0 (automatic), 4
     const bool pairs = !fp64 && is_pair_variant(variant);
     // work units: particle segments, or pair segments for the pair kernel
@@ -518,9 +561,38 @@ cudaError_t set_frame(DevTraj& d) {
 // Builds a trajectory set: allocates the store, lets `fill` write the FP64
 // points (tx, pp, aa) of N > 0 points on stream s (synchronized on return),
 // then derives the FP32 per-point data and the pair layout.
+// The order in which particles are paired: by the arrival of their first
+// point at a far observer ahead, c t - n.x, n the mean direction of the
+// first points' momenta (first[m] = t, x, y, z, bgx, bgy, bgz); particles
+// without points last.  Stable, so equal keys keep the caller's order.
+std::vector<int> pairing_order(int n_particles, const int* n_points, const double* first) {
+    std::vector<int> order(n_particles);
+    for (int m = 0; m < n_particles; m++) order[m] = m;
+    if (!first) return order;
+    double n[3] = {0.0, 0.0, 0.0};
+    for (int m = 0; m < n_particles; m++) {
+        if (n_points[m] <= 0) continue;
+        const double* f = first + 7 * (size_t)m;
+        const double b = std::sqrt(f[4] * f[4] + f[5] * f[5] + f[6] * f[6]);
+        if (b > 0.0)
+            for (int k = 0; k < 3; k++) n[k] += f[4 + k] / b;
+    }
+    const double L = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(L > 0.0)) return order;
+    std::vector<double> key(n_particles, HUGE_VAL);
+    for (int m = 0; m < n_particles; m++) {
+        if (n_points[m] <= 0) continue;
+        const double* f = first + 7 * (size_t)m;
+        key[m] = kC * f[0] - (n[0] * f[1] + n[1] * f[2] + n[2] * f[3]) / L;
+        if (!std::isfinite(key[m])) key[m] = HUGE_VAL;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    return order;
+}
+
 template <class Fill>
-int build_set(int n_particles, const int* n_points, const double* charge_C, Fill fill,
-              teufel_traj_set** out) {
+int build_set(int n_particles, const int* n_points, const double* charge_C, const double* first,
+              Fill fill, teufel_traj_set** out) {
     if (!out) return TEUFEL_ERR_ARG;
     *out = nullptr;
     if (n_particles < 0 || (n_particles > 0 && (!n_points || !charge_C))) return TEUFEL_ERR_ARG;
@@ -536,10 +608,14 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
     const int64_t N = offs[n_particles];
     // pairs (2j, 2j+1): as long as the longer particle
     const int n_pairs = (n_particles + 1) / 2;
+    const std::vector<int> order = pairing_order(n_particles, n_points, first);
+    std::vector<int> members(2 * (size_t)n_pairs + 1, -1);
     std::vector<int64_t> poffs(n_pairs + 1, 0), psegs(n_pairs + 1, 0);
     for (int j = 0; j < n_pairs; j++) {
-        int np = n_points[2 * j];
-        if (2 * j + 1 < n_particles) np = std::max(np, n_points[2 * j + 1]);
+        members[2 * j] = order[2 * j];
+        members[2 * j + 1] = 2 * j + 1 < n_particles ? order[2 * j + 1] : -1;
+        int np = n_points[members[2 * j]];
+        if (members[2 * j + 1] >= 0) np = std::max(np, n_points[members[2 * j + 1]]);
         poffs[j + 1] = poffs[j] + np;
         psegs[j + 1] = psegs[j] + (np >= 1 ? ((int64_t)(np - 1) >> kSegShift) + 1 : 0);
     }
@@ -562,6 +638,7 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
     d.n_pairs = n_pairs;
     d.n_pair_segments = psegs[n_pairs];
     int64_t *p_off, *p_seg, *p_poff, *p_pseg;
+    int* p_members;
     float4* p_pq;
     double* p_charge;
     double4_32a *p_vhat, *p_tx, *p_pp, *p_aa;
@@ -573,6 +650,7 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
         (rc = dev_alloc(h, &p_q1, N)) || (rc = dev_alloc(h, &p_q2, N)) ||
         (rc = dev_alloc(h, &p_q3, N)) || (rc = dev_alloc(h, &p_poff, n_pairs + 1)) ||
         (rc = dev_alloc(h, &p_pseg, n_pairs + 1)) ||
+        (rc = dev_alloc(h, &p_members, members.size())) ||
         (rc = dev_alloc(h, &p_pq, (size_t)kPairPoint * NP)))
         return fail(rc);
     if (cudaMalloc(&h->d_status, sizeof(unsigned int)) != cudaSuccess ||
@@ -591,12 +669,15 @@ int build_set(int n_particles, const int* n_points, const double* charge_C, Fill
     d.q3 = p_q3;
     d.pair_offsets = p_poff;
     d.pair_seg_offsets = p_pseg;
+    d.pair_members = p_members;
     d.pq = p_pq;
     cudaStream_t s = 0;
     if (cudaMemcpy(p_off, offs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
         cudaMemcpy(p_seg, segs.data(), sizeof(int64_t) * (n_particles + 1), cudaMemcpyHostToDevice) ||
         cudaMemcpy(p_poff, poffs.data(), sizeof(int64_t) * (n_pairs + 1), cudaMemcpyHostToDevice) ||
         cudaMemcpy(p_pseg, psegs.data(), sizeof(int64_t) * (n_pairs + 1), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(p_members, members.data(), sizeof(int) * members.size(),
+                   cudaMemcpyHostToDevice) ||
         (n_particles > 0 &&
          cudaMemcpy(p_charge, charge_C, sizeof(double) * n_particles, cudaMemcpyHostToDevice)) ||
         cudaMemset(h->d_status, 0, sizeof(unsigned int)))
@@ -699,7 +780,7 @@ int teufel_cuda_traj_track(int n_particles, const double* init, const double* ch
         cudaFree(buf);
         return e ? e : e2;
     };
-    return build_set(n_particles, npts.data(), charge_C.data(), fill, out);
+    return build_set(n_particles, npts.data(), charge_C.data(), init, fill, out);
 }
 
 int teufel_cuda_traj_download(const teufel_traj_set* traj, double* t, double* x, double* bg,
@@ -758,7 +839,25 @@ int teufel_cuda_traj_upload(int n_particles, const int* n_points, const double* 
         cudaFree(raw);
         return e ? e : e2;
     };
-    return build_set(n_particles, n_points, charge_C, fill, out);
+    // the first point of every particle (t, x, beta*gamma), for the pairing order
+    std::vector<double> first;
+    if (N > 0 && n_points) {
+        first.assign(7 * (size_t)n_particles, 0.0);
+        int64_t o = 0;
+        for (int m = 0; m < n_particles; m++) {
+            if (n_points[m] > 0) {
+                double* f = first.data() + 7 * (size_t)m;
+                f[0] = t[o];
+                for (int k = 0; k < 3; k++) {
+                    f[1 + k] = x[3 * o + k];
+                    f[4 + k] = bg[3 * o + k];
+                }
+            }
+            o += std::max(n_points[m], 0);
+        }
+    }
+    return build_set(n_particles, n_points, charge_C, first.empty() ? nullptr : first.data(), fill,
+                     out);
 }
 
 int teufel_cuda_traj_free(teufel_traj_set* traj) {
@@ -800,7 +899,8 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     teufel_options opt;
     teufel_cuda_default_options(&opt);
     if (opt_in) opt = *opt_in;
-    if (opt.precision != TEUFEL_PREC_FP32_SPLIT && opt.precision != TEUFEL_PREC_FP64)
+    if (opt.precision != TEUFEL_PREC_FP32_SPLIT && opt.precision != TEUFEL_PREC_FP64 &&
+        opt.precision != TEUFEL_PREC_FP32_FP64TIME)
         return TEUFEL_ERR_ARG;
     for (auto& c : h->last_counters) c = 0;
     h->last_launches = 0;
@@ -920,12 +1020,22 @@ int teufel_cuda_autotune(const teufel_traj_set* traj_c, const double* pix_pos,
     const int variants[] = {4, 7, 6, 5, 8, 1};
     float ms = 0.0f, best_t = 1e30f;
     int bv = 4, bp = 100, rc;
-    if ((rc = trial(4, 100, &ms))) return cleanup(rc);
-    for (int v : variants) {
-        if ((rc = trial(v, 100, &ms))) return cleanup(rc);
-        if (ms < best_t * kMargin || best_t == 1e30f) {
-            best_t = ms;
-            bv = v;
+    // bins short against FP64's rounding of the arrival times: only the
+    // FP64-time kernel follows the reference there
+    double t0max = 0.0;
+    if ((rc = max_abs_t0(h, d_t0, Np, s, &t0max))) return cleanup(rc);
+    if (needs_fp64_time(t0max, dt)) {
+        bv = 9;
+        if ((rc = trial(9, 100, &ms))) return cleanup(rc);
+        if ((rc = trial(9, 100, &best_t))) return cleanup(rc);
+    } else {
+        if ((rc = trial(4, 100, &ms))) return cleanup(rc);
+        for (int v : variants) {
+            if ((rc = trial(v, 100, &ms))) return cleanup(rc);
+            if (ms < best_t * kMargin || best_t == 1e30f) {
+                best_t = ms;
+                bv = v;
+            }
         }
     }
     for (int pct : {50, 200}) {
@@ -1081,7 +1191,8 @@ int teufel_cuda_record_decisions(const teufel_traj_set* traj_c, const double* pi
     if (opt.precision != TEUFEL_PREC_FP32_SPLIT) return TEUFEL_ERR_ARG;
     // the kernels the automatic choice runs: variant 4 (default) and 8
     if (opt.kernel_variant == 0) opt.kernel_variant = 4;
-    if (opt.kernel_variant != 4 && opt.kernel_variant != 8) return TEUFEL_ERR_ARG;
+    if (opt.kernel_variant != 4 && opt.kernel_variant != 8 && opt.kernel_variant != 9)
+        return TEUFEL_ERR_ARG;
     const size_t n_rec = (size_t)std::max(Np, 0) * (size_t)h->dev.n_particles *
                          (size_t)h->max_points;
     if (n_rec) std::memset(rec, 0, sizeof(int32_t) * n_rec);
