@@ -161,7 +161,8 @@ KERNEL_NAMES = {0: "lw_fp32_pair_kernel<128>", 1: "lw_fp32_warp_kernel<2>",
                 2: "lw_fp32_lanes_kernel", 3: "lw_fp32_warp_kernel<3>",
                 4: "lw_fp32_pair_kernel<128>", 5: "lw_fp32_pair_kernel<160>",
                 6: "lw_fp32_pair_kernel<136>", 7: "lw_fp32_pair_kernel<144>",
-                8: "lw_fp32_pair_kernel<128, multi-bin>"}
+                8: "lw_fp32_pair_kernel<128, multi-bin>",
+                9: "lw_fp32_pair_kernel<128, FP64 arrival times>"}
 
 
 def batch_measure(dev, reps=2, scale=64):
@@ -233,12 +234,19 @@ def other_workloads():
             tv, _, _ = ts.autotune(w.pix_pos, w.pix_t0, w.dt, w.nots)
             # after a warm-up call: the FP64 path once (seconds), the FP32 path
             # best of three (tens of milliseconds, so single runs are noisy)
-            for prec, key, reps in ((abi.PREC_FP64, "fp64", 1), (abi.PREC_FP32_SPLIT, "fp32", 3)):
-                ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
+            # where the automatic choice is the FP64-time kernel, the chained
+            # FP32 kernel (multi-bin deposits) is timed beside it
+            runs = [(abi.PREC_FP64, 0, "fp64", 1), (abi.PREC_FP32_SPLIT, 0, "fp32", 3)]
+            if tv == 9:
+                runs.append((abi.PREC_FP32_SPLIT, 8, "fp32_chained", 3))
+            for prec, variant, key, reps in runs:
+                ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec,
+                                    variant=variant)
                 best = None
                 for _ in range(reps):
                     tt = time.perf_counter()
-                    r = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec)
+                    r = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, precision=prec,
+                                            variant=variant)
                     el = time.perf_counter() - tt
                     best = el if best is None else min(best, el)
                 res[key] = (r, best)
@@ -250,6 +258,13 @@ def other_workloads():
                      "speedup_fp32_split_over_fp64": res["fp64"][1] / res["fp32"][1],
                      "rel_l2_fp32_split_vs_fp64":
                          float(np.linalg.norm(res["fp32"][0] - ref) / np.linalg.norm(ref))}
+        if "fp32_chained" in res:
+            out[name]["chained_fp32_times"] = {
+                "kernel": KERNEL_NAMES[8],
+                "evals_per_s": evals / res["fp32_chained"][1],
+                "speedup_over_fp64": res["fp64"][1] / res["fp32_chained"][1],
+                "rel_l2_vs_fp64": float(np.linalg.norm(res["fp32_chained"][0] - ref) /
+                                        np.linalg.norm(ref))}
     return out
 
 
@@ -285,6 +300,20 @@ def full_comparison():
                 el = time.perf_counter() - tt
                 t32 = el if t32 is None else min(t32, el)
             inwin, fallbacks, st = ts.last_inwindow()
+            chained = None
+            if tv == 9:
+                # the chained FP32 arrival times (multi-bin deposits) beside it
+                ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=8)
+                tc = None
+                for _ in range(2):
+                    tt = time.perf_counter()
+                    rc8 = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=8)
+                    el = time.perf_counter() - tt
+                    tc = el if tc is None else min(tc, el)
+                chained = {"kernel": KERNEL_NAMES[8], "s": tc, "evals_per_s": evals / tc,
+                           "speedup_over_fp64": t64 / tc,
+                           "rel_l2_vs_fp64": float(np.linalg.norm(rc8 - r64) / np.linalg.norm(r64))}
+                del rc8
         diff = r32 - r64
         out[name] = {"evals": evals, "pixels": w.n_pix, "particles": w.traj.n_particles,
                      "samples": w.nots, "dt": w.dt, "in_window_fraction": inwin / evals,
@@ -297,6 +326,8 @@ def full_comparison():
                          float(np.linalg.norm(diff) / np.linalg.norm(r64)),
                      "peak_sample_rel_err": float(np.abs(diff).max() / np.abs(r64).max()),
                      "tracking_s": t_track}
+        if chained:
+            out[name]["chained_fp32_times"] = chained
         del r32, r64, diff
     return out
 
