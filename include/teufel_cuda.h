@@ -48,8 +48,10 @@ extern "C" {
 #define TEUFEL_ERR_RANGE 4    /* a deposit fell outside its trace: the condition on which
                                  FieldTrace::add throws IOexception (src/fieldtrace.cpp:185-190);
                                  the offending deposit is skipped, all others are kept */
-#define TEUFEL_ERR_TIMEOUT 5  /* a device-side wait ran out; reserved: no entry point of this
-                                 library waits on the device (work queues use atomics only) */
+#define TEUFEL_ERR_TIMEOUT 5  /* a device-side wait ran out: the pair kernels wait for their
+                                 bulk copies of trajectory chunks for at most about a second
+                                 each, then stop waiting and report this (the traces are then
+                                 not to be used) */
 #define TEUFEL_ERR_NODEVICE 6 /* no CUDA device, or not an sm_103 device */
 
 /* ---- arithmetic of the integration -------------------------------------- */

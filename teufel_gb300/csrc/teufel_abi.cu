@@ -131,6 +131,7 @@ __global__ void pack_points_kernel(int64_t n, const double* t, const double* x, 
 int status_from_mask(unsigned int mask) {
     if (mask & (1u << TEUFEL_ERR_ARG)) return TEUFEL_ERR_ARG;
     if (mask & (1u << TEUFEL_ERR_RANGE)) return TEUFEL_ERR_RANGE;
+    if (mask & (1u << TEUFEL_ERR_TIMEOUT)) return TEUFEL_ERR_TIMEOUT;
     if (mask) return TEUFEL_ERR_CUDA;
     return TEUFEL_OK;
 }
