@@ -79,7 +79,9 @@ typedef struct teufel_options {
                              thread, 16/12/15/14 resident warps per SM,
                              8 = as 4, with packed deposits of steps that
                              span several bins (short bins), 9 = as 4, with
-                             the FP64 arrival times of TEUFEL_PREC_FP32_FP64TIME */
+                             the FP64 arrival times of TEUFEL_PREC_FP32_FP64TIME,
+                             10/11 = as 4, staging trajectory chunks of 8/32
+                             instead of 16 points                            */
     int timing;           /* 1: time the kernels with CUDA events on the stream,
                              read back by teufel_cuda_last_timing               */
     int max_device_mib;   /* upper bound on the device memory one call may take
@@ -89,6 +91,13 @@ typedef struct teufel_options {
                              memory.  Slots beyond the bound run as successive
                              passes; a call that cannot run one slot within it
                              returns TEUFEL_ERR_NOMEM before touching out.    */
+    int overwrite_out;    /* 1: out receives the traces instead of having them
+                             added (out is neither read nor uploaded; the
+                             result equals adding them to zeroed traces, bit
+                             for bit).  For callers whose traces were just
+                             cleared (MeshedScreen::zero, src/mesh.cpp:282-286):
+                             a host-buffer call then copies only the result
+                             back.  0 = accumulate, as FieldTrace::add does.   */
 } teufel_options;
 
 /* Fill *opt with the defaults (FP32 split path, host pointers, automatic tiling). */
@@ -206,8 +215,9 @@ int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int
 
 /* No counterpart in the reference.  Tunes the FP32 split-precision path for
  * one observer shape: times the kernel variants (warp-uniform; two particles
- * per thread at 12 to 16 resident warps per SM, and at 16 with packed
- * multi-bin deposits) at the automatic slot count -- or only the FP64-time
+ * per thread at 12 to 16 resident warps per SM, at 16 with packed
+ * multi-bin deposits, and at 16 with trajectory chunks of 8 and of 32
+ * points) at the automatic slot count -- or only the FP64-time
  * kernel (9) where TEUFEL_PREC_FP32_FP64TIME's rule selects it --
  * then the fastest at half and twice as many slots, on these very inputs,
  * writing the trial traces to a scratch buffer (out-free: nothing is added

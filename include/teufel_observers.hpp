@@ -249,8 +249,15 @@ public:
                 pos[3 * p + 2] = c.z;
                 t0[p] = CellTimeZero(ix, iy);
             }
-        check_status(teufel_cuda_integrate_screen(source->device(), pos.data(), t0.data(), dt_obs,
-                                                  (int)NOTS, (int)np, buf.data(), nullptr),
+        // traces still cleared (constructed or zero()ed): stored, not added,
+        // so that the call does not upload them
+        teufel_options opt;
+        teufel_cuda_default_options(&opt);
+        opt.overwrite_out = cleared ? 1 : 0;
+        cleared = false;
+        check_status(teufel_cuda_integrate_screen_ex(source->device(), pos.data(), t0.data(),
+                                                     dt_obs, (int)NOTS, (int)np, buf.data(), &opt,
+                                                     nullptr),
                      "ScreenObserver::integrate");
     }
 
@@ -271,6 +278,7 @@ public:
         if (size != getBufferSize())
             throw IOexception("ScreenObserver::fromBuffer() - buffer size mismatch.");
         std::memcpy(buf.data(), buffer, sizeof(double) * size);
+        cleared = false;
     }
     // The HDF5 layout of src/screen.cpp:298-560: ObservationPosition
     // [Nx][Ny][3] (attributes Nx, Ny), Screen [4][3] = origin, normal, dX, dY
@@ -309,7 +317,10 @@ public:
         }
     }
     void generateOutput() override { WriteTimeDomainFieldHDF5(); }
-    void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
+    void zero() {
+        std::fill(buf.begin(), buf.end(), 0.0);
+        cleared = true;
+    }
 
 private:
     std::string FileName;
@@ -318,6 +329,7 @@ private:
     double t0_obs, dt_obs, dtx_obs, dty_obs;
     unsigned int NOTS;
     std::vector<double> buf;  // [Nx][Ny][NOTS][6]
+    bool cleared = true;      // buf holds only zeros
 };
 
 // A screen of triangular cells, each observed at one point with its own trace
@@ -444,8 +456,13 @@ public:
             pos[3 * i + 1] = pts[i].y;
             pos[3 * i + 2] = pts[i].z;
         }
-        check_status(teufel_cuda_integrate_screen(source->device(), pos.data(), T0.data(), dt_obs,
-                                                  Nt, (int)pts.size(), buf.data(), nullptr),
+        teufel_options opt;
+        teufel_cuda_default_options(&opt);
+        opt.overwrite_out = cleared ? 1 : 0;
+        cleared = false;
+        check_status(teufel_cuda_integrate_screen_ex(source->device(), pos.data(), T0.data(),
+                                                     dt_obs, Nt, (int)pts.size(), buf.data(), &opt,
+                                                     nullptr),
                      "MeshedScreen::integrate");
     }
     std::size_t getBufferSize() override { return pts.size() * (std::size_t)Nt * 6; }
@@ -458,6 +475,7 @@ public:
         if (size != getBufferSize())
             throw IOexception("MeshedScreen::fromBuffer() - buffer size mismatch.");
         std::memcpy(buf.data(), buffer, sizeof(double) * size);
+        cleared = false;
     }
     // The HDF5 layout of src/mesh.cpp:428-736, which the file constructor
     // reads back: MeshCornerPoints [Ncp][3] (Ncp), ObservationPosition
@@ -495,7 +513,10 @@ public:
     }
     void writeFile() { writeFile(FileName); }
     void generateOutput() override { writeFile(); }
-    void zero() { std::fill(buf.begin(), buf.end(), 0.0); }
+    void zero() {
+        std::fill(buf.begin(), buf.end(), 0.0);
+        cleared = true;
+    }
 
 private:
     void load(const std::string& filename) {
@@ -542,6 +563,7 @@ private:
             v = f.read_double(f.dataset("ElMagField"));
             if (v.size() != buf.size()) throw IOexception("MeshedScreen - error reading dataset ElMagField");
             buf = std::move(v);
+            cleared = false;
         }
     }
 
@@ -553,6 +575,7 @@ private:
     double dt_obs = 0.0;
     int Nt = 0;
     std::vector<double> buf;  // [Np][Nt][6]
+    bool cleared = true;      // buf holds only zeros
     std::vector<Vector> xi, eta, normal;
     std::vector<double> area;
     double total_area = 0.0;

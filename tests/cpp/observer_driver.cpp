@@ -2,7 +2,8 @@
 // reads trajectories and an observer description from a binary file written
 // by tests/test_gpu_observers.py, runs ScreenObserver, MeshedScreen and
 // PointObserver integrate() and a SnapshotObserver on the same grid at the
-// middle of the trace window, and writes their getBuffer() contents.
+// middle of the trace window, and writes their getBuffer() contents; then the
+// mesh's buffer after a second integrate() and after zero() + integrate().
 //
 // input  (doubles unless noted): int32 n_part; int32 npts[n]; charge[n];
 //        t[N]; x[N*3]; p[N*3]; a[N*3];
@@ -102,6 +103,17 @@ int main(int argc, char** argv) {
         snap.integrate();
         b = snap.getBuffer();
         fwrite(b, sizeof(double), snap.getBufferSize(), out);
+        delete[] b;
+        // the mesh integrated a second time (added to its traces), then
+        // cleared and integrated again (stored)
+        mesh.integrate();
+        b = mesh.getBuffer();
+        fwrite(b, sizeof(double), mesh.getBufferSize(), out);
+        delete[] b;
+        mesh.zero();
+        mesh.integrate();
+        b = mesh.getBuffer();
+        fwrite(b, sizeof(double), mesh.getBufferSize(), out);
         delete[] b;
     } catch (const IOexception& e) {
         fprintf(stderr, "IOexception: %s\n", e.what());

@@ -17,7 +17,7 @@ def test_autotune_choice_and_parity():
     assert rc == 0
     with abi.TrajSet(w.traj) as ts:
         variant, slots, ms = ts.autotune(w.pix_pos, w.pix_t0, w.dt, w.nots)
-        assert variant in (1, 4, 5, 6, 7, 8) and slots >= 1 and ms > 0.0
+        assert variant in (1, 4, 5, 6, 7, 8, 10, 11) and slots >= 1 and ms > 0.0
         g = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots)  # automatic: the tuned choice
         g2 = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, variant=variant,
                                  n_slots=slots)

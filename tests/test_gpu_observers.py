@@ -47,7 +47,17 @@ def test_cpp_observers_match_oracle(tmp_path):
     screen = data[:n].reshape(w.n_pix, w.nots, 6)
     mesh = data[n:2 * n].reshape(w.n_pix, w.nots, 6)
     point = data[2 * n:2 * n + w.nots * 6].reshape(w.nots, 6)
-    snap = data[2 * n + w.nots * 6:].reshape(s.nx * s.ny, 6)
+    m = 2 * n + w.nots * 6
+    snap = data[m:m + s.nx * s.ny * 6].reshape(s.nx * s.ny, 6)
+    m += s.nx * s.ny * 6
+    mesh_twice = data[m:m + n].reshape(w.n_pix, w.nots, 6)
+    mesh_again = data[m + n:].reshape(w.n_pix, w.nots, 6)
+    # the first integrate() after construction or zero() stores the traces
+    # (overwrite_out), a later one adds them: twice the traces, then the same
+    # traces again, bit for bit
+    assert mesh_again.shape == mesh.shape
+    assert np.array_equal(mesh_twice, 2.0 * mesh)
+    assert np.array_equal(mesh_again, mesh)
     ref, rc = lw.integrate_screen(tr, w.pix_pos, w.pix_t0, w.dt, w.nots)
     assert rc == 0
     nrm = np.linalg.norm(ref)

@@ -72,7 +72,7 @@ def test_config1_fp64_matches_oracle(c1, c1_oracle):
     assert inwin > 0
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4, 8])
+@pytest.mark.parametrize("variant", [1, 2, 4, 8, 10, 11])
 def test_config1_fp32_matches_oracle(c1, c1_oracle, variant):
     with abi.TrajSet(c1.traj) as ts:
         g = ts.integrate_screen(c1.pix_pos, c1.pix_t0, c1.dt, c1.nots, variant=variant)
@@ -293,7 +293,7 @@ def _truncated(traj, lengths):
                           np.array(ms))
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4, 8])
+@pytest.mark.parametrize("variant", [1, 2, 4, 8, 10, 11])
 def test_uneven_particle_set(variant):
     """An odd number of particles of unequal lengths, one with a single point
     and one with none: the pair kernel pads the shorter particle of a pair
@@ -538,3 +538,56 @@ def test_many_wave_grid_with_geometric_slots():
         b = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots, n_slots=64)
     assert np.array_equal(a, b)
     assert rel_l2(a, ref) < TOL_FP32, rel_l2(a, ref)
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP32_SPLIT, abi.PREC_FP64])
+def test_overwrite_out(c1, precision):
+    """overwrite_out stores the traces: into a buffer of garbage (never read
+    or uploaded) they equal, bit for bit, the traces added to zeros; with a
+    device-memory bound that runs three passes, the first stores and the
+    others add; a trace shorter than 2 samples or an empty set leaves zeros."""
+    sel = np.arange(0, c1.n_pix, 3)
+    pos, t0 = c1.pix_pos[sel], c1.pix_t0[sel]
+    garbage = np.random.default_rng(9).normal(size=(len(sel), c1.nots, 6)) * 1e30
+    slot = len(sel) * c1.nots * 6 * (4 if precision == abi.PREC_FP32_SPLIT else 8)
+    staged = 8 * (4 * len(sel) + len(sel) * c1.nots * 6)
+    mib = (staged + 2 * slot) // (1 << 20) + 1
+    with abi.TrajSet(c1.traj) as ts:
+        ref = ts.integrate_screen(pos, t0, c1.dt, c1.nots, precision=precision)
+        g = ts.integrate_screen(pos, t0, c1.dt, c1.nots, out=garbage.copy(), precision=precision,
+                                overwrite_out=True)
+        ref_b = ts.integrate_screen(pos, t0, c1.dt, c1.nots, precision=precision, n_slots=6,
+                                    max_device_mib=mib)
+        g_b = ts.integrate_screen(pos, t0, c1.dt, c1.nots, out=garbage.copy(),
+                                  precision=precision, n_slots=6, max_device_mib=mib,
+                                  overwrite_out=True)
+        _, _, launches, _, _ = ts.last_timing()
+        short = ts.integrate_screen(pos[:3], t0[:3], c1.dt, 1, out=np.ones((3, 1, 6)),
+                                    overwrite_out=True)
+    assert np.abs(ref).max() > 0
+    assert np.array_equal(g, ref)
+    assert launches == 6  # three passes of (integration, reduction)
+    assert np.array_equal(g_b, ref_b)
+    assert np.all(short == 0.0)
+    empty = H.Trajectories(np.zeros(0), np.zeros((0, 3)), np.zeros((0, 3)), np.zeros((0, 3)),
+                           np.zeros(0, np.int32), np.zeros(0), np.zeros(0))
+    with abi.TrajSet(empty) as ts:
+        e = ts.integrate_screen(pos[:2], t0[:2], c1.dt, 8, out=np.ones((2, 8, 6)),
+                                overwrite_out=True)
+    assert np.all(e == 0.0)
+
+
+def test_overwrite_out_device_pointers(c1):
+    import torch
+    dev = torch.device("cuda", 0)
+    pos = torch.from_numpy(np.ascontiguousarray(c1.pix_pos)).to(dev)
+    t0 = torch.from_numpy(np.ascontiguousarray(c1.pix_t0)).to(dev)
+    acc = torch.zeros((c1.n_pix, c1.nots, 6), dtype=torch.float64, device=dev)
+    ovw = torch.full_like(acc, float("nan"))
+    with abi.TrajSet(c1.traj) as ts:
+        ts.integrate_screen_device(pos.data_ptr(), t0.data_ptr(), c1.dt, c1.nots, c1.n_pix,
+                                   acc.data_ptr())
+        ts.integrate_screen_device(pos.data_ptr(), t0.data_ptr(), c1.dt, c1.nots, c1.n_pix,
+                                   ovw.data_ptr(), overwrite_out=True)
+        torch.cuda.synchronize(dev)
+    assert torch.equal(acc, ovw)

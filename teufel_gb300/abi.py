@@ -48,7 +48,8 @@ NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("n_slots", ctypes.c_int), ("kernel_variant", ctypes.c_int),
-                ("timing", ctypes.c_int), ("max_device_mib", ctypes.c_int)]
+                ("timing", ctypes.c_int), ("max_device_mib", ctypes.c_int),
+                ("overwrite_out", ctypes.c_int)]
 
 
 class ObserverDesc(ctypes.Structure):
@@ -193,7 +194,7 @@ def _ptr(a, t=_dp):
 
 def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
             n_slots: int = 0, timing: bool = False, variant: int = 0,
-            max_device_mib: int = 0) -> Options:
+            max_device_mib: int = 0, overwrite_out: bool = False) -> Options:
     o = Options()
     lib().teufel_cuda_default_options(ctypes.byref(o))
     o.precision = precision
@@ -202,6 +203,7 @@ def options(precision: int = PREC_FP32_SPLIT, device_pointers: bool = False,
     o.timing = 1 if timing else 0
     o.kernel_variant = variant
     o.max_device_mib = max_device_mib
+    o.overwrite_out = 1 if overwrite_out else 0
     return o
 
 
@@ -284,9 +286,11 @@ class TrajSet:
     def integrate_screen(self, pix_pos, pix_t0, dt, nots, out=None,
                          precision: int = PREC_FP32_SPLIT, n_slots: int = 0,
                          stream: int = 0, variant: int = 0,
-                         max_device_mib: int = 0) -> np.ndarray:
+                         max_device_mib: int = 0, overwrite_out: bool = False) -> np.ndarray:
         """Traces of all particles on the pixels, added into ``out``
-        ([Np][nots][6] doubles, zeros if None) -- host buffers."""
+        ([Np][nots][6] doubles, zeros if None) -- host buffers.  With
+        ``overwrite_out`` they are stored into ``out`` instead (its contents
+        neither read nor uploaded)."""
         pix_pos = _c(pix_pos).reshape(-1, 3)
         pix_t0 = _c(pix_t0).reshape(-1)
         n_pix = pix_pos.shape[0]
@@ -294,7 +298,8 @@ class TrajSet:
             out = np.zeros((n_pix, nots, 6))
         if not (out.dtype == np.float64 and out.flags.c_contiguous):
             raise ValueError("out must be a C-contiguous float64 array")
-        opt = options(precision, False, n_slots, variant=variant, max_device_mib=max_device_mib)
+        opt = options(precision, False, n_slots, variant=variant, max_device_mib=max_device_mib,
+                      overwrite_out=overwrite_out)
         check(lib().teufel_cuda_integrate_screen_ex(self.handle, pix_pos.ctypes.data,
                                                     pix_t0.ctypes.data, dt, nots, n_pix,
                                                     out.ctypes.data, ctypes.byref(opt),
@@ -305,9 +310,9 @@ class TrajSet:
     def integrate_screen_device(self, pos_ptr: int, t0_ptr: int, dt: float, nots: int,
                                 n_pix: int, out_ptr: int, precision: int = PREC_FP32_SPLIT,
                                 n_slots: int = 0, stream: int = 0, timing: bool = False,
-                                variant: int = 0) -> None:
+                                variant: int = 0, overwrite_out: bool = False) -> None:
         """Device-pointer variant; returns once the work is enqueued."""
-        opt = options(precision, True, n_slots, timing, variant)
+        opt = options(precision, True, n_slots, timing, variant, overwrite_out=overwrite_out)
         check(lib().teufel_cuda_integrate_screen_ex(self.handle, _vp(pos_ptr), _vp(t0_ptr), dt,
                                                     nots, n_pix, _vp(out_ptr),
                                                     ctypes.byref(opt), _vp(stream)),

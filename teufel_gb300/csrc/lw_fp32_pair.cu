@@ -600,24 +600,27 @@ constexpr int kPThreads = kPairTile;  // one warp per block: residency is set by
 // within 10 KB per block, so 16 one-warp blocks fit an SM's shared memory.
 // Anchors may move at chunk boundaries; segment boundaries stay chunk
 // boundaries.
+// The chunk length is a template parameter CS (2^CS pair-points) the
+// autotuner searches: 8, 16 (the default) or 32.
 constexpr int kPChunkShift = 4;
-constexpr int kPChunkLen = 1 << kPChunkShift;
-static_assert(kSegLen % kPChunkLen == 0 && kPChunkLen % 2 == 0, "chunk layout");
 
 // A staged chunk: p[l] is the chunk's point l.
-struct __align__(16) PairChunk {
-    PairPoint p[kPChunkLen];
+template <int CS>
+struct __align__(16) PairChunkT {
+    static_assert(kSegLen % (1 << CS) == 0 && (1 << CS) % 2 == 0, "chunk layout");
+    PairPoint p[1 << CS];
 };
 
 // The 32 lanes copy pair-points p0 .. p0+avail-1 of the pair whose data
 // starts at pq.
-__device__ __forceinline__ void pair_stage(PairChunk* b, const float4* pq, int p0, int avail,
+template <int CS>
+__device__ __forceinline__ void pair_stage(PairChunkT<CS>* b, const float4* pq, int p0, int avail,
                                            int lane) {
     const int n = kPairPoint * avail;
     const float4* src = pq + kPairPoint * (int64_t)p0;
     float4* dst = reinterpret_cast<float4*>(b->p);
 #pragma unroll
-    for (int k = 0; k < (kPairPoint * kPChunkLen + 31) / 32; k++) {
+    for (int k = 0; k < ((kPairPoint << CS) + 31) / 32; k++) {
         const int t = lane + 32 * k;
         if (t < n) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + t);
@@ -647,7 +650,8 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar) {
 __device__ __forceinline__ void mbar_inval(unsigned long long* bar) {
     asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-__device__ __forceinline__ void bulk_stage(PairChunk* b, const float4* pq, int p0, int avail,
+template <int CS>
+__device__ __forceinline__ void bulk_stage(PairChunkT<CS>* b, const float4* pq, int p0, int avail,
                                            unsigned long long* bar) {
     const unsigned bytes = (unsigned)(avail * kPairPoint * sizeof(float4));
     unsigned long long src;
@@ -720,8 +724,9 @@ struct PairWalk {
 };
 
 // Shared memory of one block (one warp).
-struct PairShared {
-    PairChunk buf[2];
+template <int CS>
+struct PairSharedT {
+    PairChunkT<CS> buf[2];
     PixelCtx px[kPThreads];
     PairWalk walk;
     unsigned long long stats[2];  // point evaluations, exact fallbacks
@@ -731,10 +736,12 @@ struct PairShared {
 // One pixel tile (kPThreads pixels of the observer) against one slot of the
 // trajectory set: the whole work of a block of the per-observer kernel, and
 // one work item of the batched kernel.
-template <bool PINGPONG, bool MULTI, bool REC, bool EXACT = false>
+template <bool PINGPONG, bool MULTI, bool REC, bool EXACT = false, int CS = kPChunkShift>
 __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
                                           const DevWork& wk, int slot, int tile,
-                                          PairShared& sh) {
+                                          PairSharedT<CS>& sh) {
+    constexpr int kPChunkLen = 1 << CS;
+    using PairChunk = PairChunkT<CS>;
     const int pix = tile * kPThreads + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int np = sc.np;
@@ -984,9 +991,9 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 
         const std::integral_constant<bool, true> kFresh;
         const std::integral_constant<bool, false> kChained;
-        const int n_chunks = (W.n_pts + kPChunkLen - 1) >> kPChunkShift;
+        const int n_chunks = (W.n_pts + kPChunkLen - 1) >> CS;
         for (int c = 0; c < n_chunks; c++) {
-            const int p0 = start + (c << kPChunkShift);
+            const int p0 = start + (c << CS);
             if constexpr (kBulkStage) {
                 if (c + 1 < n_chunks && lane == 0 && !stalled)
                     bulk_stage(&wb[(c + 1) & 1], W.pq, p0 + kPChunkLen,
@@ -1031,7 +1038,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 }
                 A = An;
             }
-            const int n_here = min(kPChunkLen, W.n_pts - (c << kPChunkShift));
+            const int n_here = min(kPChunkLen, W.n_pts - (c << CS));
             int l = 0;
             if (c == 0) {
                 // the walk's first point: no step ends there
@@ -1127,11 +1134,14 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
 // EXACT: the FP64-time mode (FP32 fields, the reference's FP64 arrival times,
 // bins and bin edges), for observers whose bins are so short that FP64's own
 // rounding of the arrival times is not negligible against them.
-template <int MAXREG, bool PINGPONG, bool MULTI = false, bool REC = false, bool EXACT = false>
+//
+// CS: chunks of 2^CS pair-points (8, 16 or 32).
+template <int MAXREG, bool PINGPONG, bool MULTI = false, bool REC = false, bool EXACT = false,
+          int CS = kPChunkShift>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
-    __shared__ PairShared sh;
-    pair_tile<PINGPONG, MULTI, REC, EXACT>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
+    __shared__ PairSharedT<CS> sh;
+    pair_tile<PINGPONG, MULTI, REC, EXACT, CS>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
 }
 
 // Persistent form: every block takes (observer, tile, slot) items from the
@@ -1140,7 +1150,7 @@ template <int MAXREG, bool REC = false>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_batch_kernel(const DevTraj* trs, const DevScreen* scs, const DevWork* wks,
                               const BatchItem* items, int n_items, unsigned int* head) {
-    __shared__ PairShared sh;
+    __shared__ PairSharedT<kPChunkShift> sh;
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned int it = 0;
@@ -1192,6 +1202,14 @@ cudaError_t launch_fp32_pair(const DevTraj& tr, const DevScreen& sc, const DevWo
             lw_fp32_pair_kernel<128, false, false, false, true><<<grid, kPThreads, 0, s>>>(tr, sc,
                                                                                          w);
             break;
+        case kVariantPairC8:
+            lw_fp32_pair_kernel<128, false, false, false, false, 3><<<grid, kPThreads, 0, s>>>(
+                tr, sc, w);
+            break;
+        case kVariantPairC32:
+            lw_fp32_pair_kernel<128, false, false, false, false, 5><<<grid, kPThreads, 0, s>>>(
+                tr, sc, w);
+            break;
         default:
             lw_fp32_pair_kernel<128, false><<<grid, kPThreads, 0, s>>>(tr, sc, w);
             break;
@@ -1204,10 +1222,11 @@ int pair_batch_blocks_per_sm() { return 65536 / (32 * kBatchMaxReg); }
 
 int pair_blocks_per_sm(int variant) {
     // occupancy of the kernel of each variant, asked once
-    static int cached[6] = {-1, -1, -1, -1, -1, -1};
+    static int cached[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
     const int k = variant == kVariantPair160 ? 1 : variant == kVariantPair136 ? 2
                 : variant == kVariantPair144 ? 3 : variant == kVariantPairMulti ? 4
-                : variant == kVariantPairTime ? 5 : 0;
+                : variant == kVariantPairTime ? 5 : variant == kVariantPairC8 ? 6
+                : variant == kVariantPairC32 ? 7 : 0;
     if (cached[k] >= 0) return cached[k];
     int n = 0;
     cudaError_t e;
@@ -1231,6 +1250,14 @@ int pair_blocks_per_sm(int variant) {
         case 5:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &n, lw_fp32_pair_kernel<128, false, false, false, true>, kPThreads, 0);
+            break;
+        case 6:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &n, lw_fp32_pair_kernel<128, false, false, false, false, 3>, kPThreads, 0);
+            break;
+        case 7:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &n, lw_fp32_pair_kernel<128, false, false, false, false, 5>, kPThreads, 0);
             break;
         default:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lw_fp32_pair_kernel<128, false>,

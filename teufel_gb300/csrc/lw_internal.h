@@ -110,6 +110,9 @@ struct DevWork {
     // encoded by rec_encode.
     int* rec;
     int64_t rec_stride;
+    // 1: the reduction stores the traces into out (out treated as zero)
+    // instead of adding them
+    int overwrite;
 };
 
 // A point decision as recorded: bin index + 4 in bits 0-26, the window and
@@ -144,7 +147,10 @@ constexpr int kVariantPairMulti = 7;
 // times and bin edges (where FP64's own rounding of the arrival times is not
 // negligible against the bin width)
 constexpr int kVariantPairTime = 8;
-constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPairTime; }
+// as kVariantPair, with chunks of 8 / 32 pair-points instead of 16
+constexpr int kVariantPairC8 = 9;
+constexpr int kVariantPairC32 = 10;
+constexpr bool is_pair_variant(int v) { return v >= kVariantPair && v <= kVariantPairC32; }
 cudaError_t launch_fp32(const DevTraj& tr, const DevScreen& sc, const DevWork& w, int variant,
                         cudaStream_t s);
 cudaError_t launch_fp32_warp(const DevTraj& tr, const DevScreen& sc, const DevWork& w,

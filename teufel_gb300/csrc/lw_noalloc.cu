@@ -131,7 +131,7 @@ extern "C" int teufel_cuda_integrate_screen_noalloc(const teufel_traj_set* traj,
         // the bounds live on the host stack: wait for the copy before reusing them
         if (!e) e = cudaStreamSynchronize(s);
         if (e) return fail(e);
-        DevWork w;
+        DevWork w{};
         w.n_slots = n;
         w.slot_seg = sym->slot_seg;
         w.scratch = sym->scratch;

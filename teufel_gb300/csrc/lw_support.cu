@@ -58,12 +58,19 @@ __device__ __forceinline__ void reduce_fp32_bin(const DevWork& w, int64_t e, dou
     // quotient; an FP64 division costs ten times as much)
     constexpr double kInvC = 1.0 / kC;
     double* o = out + e * 6;
-    o[0] += acc[0];
-    o[1] += acc[1];
-    o[2] += acc[2];
-    o[3] += acc[3] * kInvC;
-    o[4] += acc[4] * kInvC;
-    o[5] += acc[5] * kInvC;
+    // overwrite: out is taken as zero and not read (0.0 + x, so that a -0.0
+    // leaves as +0.0, exactly as when it is added to zeroed traces)
+    double b[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (!w.overwrite) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) b[k] = o[k];
+    }
+    o[0] = b[0] + acc[0];
+    o[1] = b[1] + acc[1];
+    o[2] = b[2] + acc[2];
+    o[3] = b[3] + acc[3] * kInvC;
+    o[4] = b[4] + acc[4] * kInvC;
+    o[5] = b[5] + acc[5] * kInvC;
 }
 
 // bins [e0, e1) of the observer
@@ -112,7 +119,7 @@ __global__ void reduce_fp64_kernel(DevWork w, int64_t e0, int64_t e1, double* ou
         }
         double* o = out + e * 6;
 #pragma unroll
-        for (int c = 0; c < 6; c++) o[c] += acc[c];
+        for (int c = 0; c < 6; c++) o[c] = (w.overwrite ? 0.0 : o[c]) + acc[c];
     }
 }
 

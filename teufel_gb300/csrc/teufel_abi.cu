@@ -358,6 +358,8 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                         : opt.kernel_variant == 7 ? kVariantPair144
                         : opt.kernel_variant == 8 ? kVariantPairMulti
                         : opt.kernel_variant == 9 ? kVariantPairTime
+                        : opt.kernel_variant == 10 ? kVariantPairC8
+                        : opt.kernel_variant == 11 ? kVariantPairC32
                                                   : kVariantPair;  // 0 (automatic), 4
     const bool pairs = !fp64 && is_pair_variant(variant);
     // work units: particle segments, or pair segments for the pair kernel
@@ -435,8 +437,10 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     }
     DevScreen sc{d_pos, d_t0, np, nt, dt};
     for (int64_t p0 = 0; p0 < slots_total; p0 += per_pass) {
-        DevWork w;
+        DevWork w{};
         w.n_slots = (int)std::min<int64_t>(per_pass, slots_total - p0);
+        // the first pass stores the traces when asked to, the others add
+        w.overwrite = opt.overwrite_out && p0 == 0;
         w.slot_seg = h->slot_seg + p0;
         w.scratch = scratch;
         w.slot_stride = (int64_t)np * nt * 6;
@@ -450,7 +454,7 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
                              : launch_fp32(h->dev, sc, w, variant, s);
         if (e != cudaSuccess) return cuda_fail(e);
         if (h->last_timed) TRY_CUDA(cudaEventRecord(h->ev[h->n_ev_used + 1], s));
-        if (ho && p0 == 0) TRY_CUDA(cudaStreamWaitEvent(s, ho->uploaded, 0));
+        if (ho && p0 == 0 && !opt.overwrite_out) TRY_CUDA(cudaStreamWaitEvent(s, ho->uploaded, 0));
         if (ho && p0 + per_pass >= slots_total) {
             const int64_t n_bins = (int64_t)np * nt;
             for (int k = 0; k < ho->n_chunks; k++) {
@@ -720,6 +724,7 @@ void teufel_cuda_default_options(teufel_options* opt) {
     opt->kernel_variant = 0;
     opt->timing = 0;
     opt->max_device_mib = 0;
+    opt->overwrite_out = 0;
 }
 
 const char* teufel_cuda_status_string(int status) {
@@ -906,11 +911,23 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     for (auto& c : h->last_counters) c = 0;
     h->last_launches = 0;
     h->n_ev_used = 0;
-    // the reference returns early for traces shorter than 2 samples and for
-    // trajectories shorter than 2 points (src/particle.cpp:778, 783)
-    if (Nt < 2 || Np == 0 || h->dev.n_particles == 0 || h->dev.n_segments == 0) return TEUFEL_OK;
-    if (!(dt > 0.0) && !(dt < 0.0)) return TEUFEL_ERR_ARG;
+    if (opt.overwrite_out != 0 && opt.overwrite_out != 1) return TEUFEL_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the reference returns early for traces shorter than 2 samples and for
+    // trajectories shorter than 2 points (src/particle.cpp:778, 783): out
+    // keeps its values, or holds zeros when it is to be overwritten
+    if (Nt < 2 || Np == 0 || h->dev.n_particles == 0 || h->dev.n_segments == 0) {
+        if (opt.overwrite_out && Np > 0 && Nt > 0) {
+            const size_t n = sizeof(double) * 6 * (size_t)Np * (size_t)Nt;
+            if (opt.device_pointers) {
+                TRY_CUDA(cudaMemsetAsync(out, 0, n, s));
+            } else {
+                std::memset(out, 0, n);
+            }
+        }
+        return TEUFEL_OK;
+    }
+    if (!(dt > 0.0) && !(dt < 0.0)) return TEUFEL_ERR_ARG;
     int rc;
     if (opt.device_pointers) {
         return run_device(h, pix_pos, pix_t0, dt, Nt, Np, out, opt, s);
@@ -941,8 +958,10 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
     TRY_CUDA(cudaStreamWaitEvent(h->copy_s, h->cev[0], 0));
     TRY_CUDA(cudaMemcpyAsync(d_pos, pix_pos, sizeof(double) * 3 * Np, cudaMemcpyHostToDevice, s));
     TRY_CUDA(cudaMemcpyAsync(d_t0, pix_t0, sizeof(double) * Np, cudaMemcpyHostToDevice, s));
-    TRY_CUDA(cudaMemcpyAsync(h->d_out, out, sizeof(double) * nout, cudaMemcpyHostToDevice,
-                             h->copy_s));
+    // out is uploaded only when the traces are added to it
+    if (!opt.overwrite_out)
+        TRY_CUDA(cudaMemcpyAsync(h->d_out, out, sizeof(double) * nout, cudaMemcpyHostToDevice,
+                                 h->copy_s));
     TRY_CUDA(cudaEventRecord(h->cev[1], h->copy_s));
     const HostOut ho{out, h->copy_s, h->cev[1], h->cev.data() + 3, kOutChunks};
     rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s, 100, &ho, nullptr, staged);
@@ -1018,7 +1037,7 @@ int teufel_cuda_autotune(const teufel_traj_set* traj_c, const double* pix_pos,
     // vary by a few tenths of a percent, and ties go to the default kernel
     // and the automatic slot count.
     constexpr float kMargin = 0.995f;
-    const int variants[] = {4, 7, 6, 5, 8, 1};
+    const int variants[] = {4, 7, 6, 5, 8, 10, 11, 1};
     float ms = 0.0f, best_t = 1e30f;
     int bv = 4, bp = 100, rc;
     // bins short against FP64's rounding of the arrival times: only the
