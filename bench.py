@@ -38,10 +38,11 @@ UNIT = "evals/s"
 FLOPS_PER_STEP = 110.0
 FLOPS_PER_EXTRA_BIN = 14.0
 # DRAM bytes (read + write) per in-window (pixel, particle, step) of the pair
-# kernel, from a one-pass ncu capture of one full-size bench launch (1024
-# particles, 40000 pixels, 4096 samples, 9 slots): 1.436e12 B / 9.93e10
-# in-window steps
-DRAM_BYTES_PER_INWINDOW_STEP = 14.47
+# kernel, from an ncu capture of one launch on 1250 of the 40000 pixels (the
+# bench's 1024 particles, 4096 samples and 9 slots): 23.46e9 B / 3.101e9
+# in-window steps.  Nothing of the partial traces is reused from L2 at either
+# size, so the per-step figure carries over to the full launch.
+DRAM_BYTES_PER_INWINDOW_STEP = 7.57
 
 
 def parse():
@@ -673,10 +674,11 @@ def run_gb300(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 else None,
                          "traffic": DRAM_BYTES_PER_INWINDOW_STEP * inwin / max(K, 1),
-                         "traffic_note": "DRAM bytes per launch: 14.47 B per in-window "
-                                         "step (dram__bytes_read.sum + write.sum of one "
-                                         "full-size launch, one ncu pass) times the in-window "
-                                         "steps of one launch",
+                         "traffic_note": f"DRAM bytes per launch: "
+                                         f"{DRAM_BYTES_PER_INWINDOW_STEP} B per in-window step "
+                                         "(dram__bytes_read.sum + write.sum of one launch on "
+                                         "1250 of the 40000 pixels, 1024 particles, 9 slots) "
+                                         "times the in-window steps of one full launch",
                          "kernel": KERNEL_NAMES.get(tuned["kernel_variant"] if tuned
                                                     else args.variant, "?"),
                          "peak_source": "the larger of the FFMA and packed-FFMA2 throughput "
