@@ -845,28 +845,45 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         };
 
         // The FP64-time mode: point i of particle w resolved with the
-        // reference's arrival time, and the step from q1 deposited on it
-        // (ka/kb then hold the bin itself, exa/exb its encoded decision).
+        // reference's arrival time (exa/exb then hold its encoded bin and
+        // flags; 0 = not resolved), and the step from q1 deposited on it.
         auto ftime_point = [&](auto& q, int w, int i) {
             const double ts = exact_retarded_time(w ? W.txb[i] : W.txa[i], px.P);
-            const int idx = exact_bin(ts, px.w);
-            const int ex = rec_encode(idx, exact_flags(ts, px.w));
+            const int ex = rec_encode(exact_bin(ts, px.w), exact_flags(ts, px.w));
             if (w) {
                 q.tsb = ts;
-                q.kb = idx;
                 q.exb = ex;
             } else {
                 q.tsa = ts;
-                q.ka = idx;
                 q.exa = ex;
             }
+            if constexpr (REC) {
+                if (w) record_point<1>(wk, tr.n_particles, pix, mb, i, q, 0, nt);
+                else record_point<0>(wk, tr.n_particles, pix, ma, i, q, 0, nt);
+            }
         };
-        auto ftime_step = [&](auto wtag, const auto& q1, auto& q2, int i) {
+        // Only steps that can reach the window resolve their points: the
+        // FP32 chain places every point within chain_err (a few 1e-5) of its
+        // bin coordinate, so a point whose chained bin is <= -2 lies before
+        // tmin (bin edge -1/2), and one whose bin is >= nt + 1 at or after
+        // tmax (edge nt - 1/2).  A step ending before the window or starting
+        // after it deposits nothing (src/particle.cpp:793), and the
+        // accumulator is then empty: arrivals increase along the walk.
+        auto ftime_step = [&](auto wtag, auto& q1, auto& q2, int i) {
             constexpr int Wp = decltype(wtag)::value;
+            const int k1 = Wp ? A.Bb + q1.kb : A.Ba + q1.ka;
+            const int k2 = Wp ? A.Bb + q2.kb : A.Ba + q2.ka;
+            const bool sure = (Wp ? chain_err.v.y : chain_err.v.x) < 0.25f &&
+                              fabsf(Wp ? q1.r.v.y : q1.r.v.x) <= 0.5f &&
+                              fabsf(Wp ? q2.r.v.y : q2.r.v.x) <= 0.5f;
+            if (sure && (k2 <= -2 || k1 >= nt + 1)) return;
+            if (!(Wp ? q1.exb : q1.exa)) ftime_point(q1, Wp, i - 1);
             ftime_point(q2, Wp, i);
-            const int idx1 = Wp ? q1.kb : q1.ka, idx2 = Wp ? q2.kb : q2.ka;
-            const int fl1 = (Wp ? q1.exb : q1.exa) >> kRecFlagShift;
-            const int fl2 = (Wp ? q2.exb : q2.exa) >> kRecFlagShift;
+            const int e1 = Wp ? q1.exb : q1.exa, e2 = Wp ? q2.exb : q2.exa;
+            const int idx1 = (e1 & ((1 << kRecFlagShift) - 1)) - 4;
+            const int idx2 = (e2 & ((1 << kRecFlagShift) - 1)) - 4;
+            const int fl1 = e1 >> kRecFlagShift;
+            const int fl2 = e2 >> kRecFlagShift;
             float2 f1[3], f2[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -893,17 +910,6 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         auto step = [&](auto fresh, PS& q1, PS& q2, const PairChunk& B, int l, int i) {
             F2 aminus;
             point_field2(q2, B.p[l], A, aminus);
-            if constexpr (EXACT) {
-                // FP32 fields, the reference's FP64 arrival times: the bin and
-                // flags of every point are the reference's
-                if (i <= lim_a) ftime_step(kPa, q1, q2, i);
-                if (i <= lim_b) ftime_step(kPb, q1, q2, i);
-                if constexpr (REC) {
-                    if (i <= lim_a) record_point<0>(wk, tr.n_particles, pix, ma, i, q2, 0, nt);
-                    if (i <= lim_b) record_point<1>(wk, tr.n_particles, pix, mb, i, q2, 0, nt);
-                }
-                return;
-            }
             q2.exa = q2.exb = 0;
             if constexpr (decltype(fresh)::value) {
                 start_chain2(q2, A);
@@ -914,6 +920,13 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 chain_step2(q1, q2, du, comp);
                 // du >= 0: arrivals increase along the points
                 chain_err = fma(du, f2(kChainRel, kChainRel), chain_err + f2(1.0e-7f, 1.0e-7f));
+            }
+            if constexpr (EXACT) {
+                // FP32 fields, the reference's FP64 arrival times: the bin and
+                // flags of every point that can deposit are the reference's
+                if (i <= lim_a) ftime_step(kPa, q1, q2, i);
+                if (i <= lim_b) ftime_step(kPb, q1, q2, i);
+                return;
             }
             // the step ending at point i belongs to this lane and slot
             const bool dep_a = i <= lim_a, dep_b = i <= lim_b;
@@ -1016,9 +1029,11 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             }
             __syncwarp();
             const PairChunk& B = wb[c & 1];
+            // (the FP64-time mode needs the chain only to a fraction of a bin)
             const bool anchor =
                 c == 0 || (p0 & (kSegLen - 1)) == 0 ||
-                warp_any_above(fmaxf(chain_err.v.x, chain_err.v.y), kReanchorBound);
+                warp_any_above(fmaxf(chain_err.v.x, chain_err.v.y),
+                               EXACT ? 0.01f : kReanchorBound);
             if (anchor) {
                 Anchor aa, ab;
                 // past its last point a particle repeats it, with positions
@@ -1031,7 +1046,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 else ab = aa;
                 if (wa <= 0) aa = ab;
                 const Anchor2 An = pack_anchor(aa, ab);
-                if (c > 0 && !EXACT) {
+                if (c > 0) {
                     // rebase the previous point: B + k is unchanged
                     p1.ka += A.Ba - An.Ba;
                     p1.kb += A.Bb - An.Bb;
@@ -1049,14 +1064,13 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                 comp = f2(0.0f, 0.0f);
                 chain_err = A.err;
                 if constexpr (EXACT) {
-                    if (start <= lim_a) ftime_point(p1, 0, start);
-                    if (start <= lim_b) ftime_point(p1, 1, start);
+                    // resolved by the first step that can deposit
                 } else {
                     const int2 nr = near(p1);
                     if (nr.x && start <= lim_a) resolve(p1, 0, start);
                     if (nr.y && start <= lim_b) resolve(p1, 1, start);
                 }
-                if constexpr (REC) {
+                if constexpr (REC && !EXACT) {
                     if (start <= lim_a)
                         record_point<0>(wk, tr.n_particles, pix, ma, start, p1, A.Ba, nt);
                     if (start <= lim_b)
@@ -1094,7 +1108,12 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         // what the accumulators still hold belongs to the bins of the walk's
         // last point
         {
-            const int ka = EXACT ? p1.ka : A.Ba + p1.ka, kb = EXACT ? p1.kb : A.Bb + p1.kb;
+            // (FP64-time mode: the bins of the resolved point; an unresolved
+            // one ends a walk whose accumulator is empty)
+            const int ka = EXACT ? (p1.exa ? (p1.exa & ((1 << kRecFlagShift) - 1)) - 4 : -1)
+                                 : A.Ba + p1.ka;
+            const int kb = EXACT ? (p1.exb ? (p1.exb & ((1 << kRecFlagShift) - 1)) - 4 : -1)
+                                 : A.Bb + p1.kb;
             s.reduce_if<0>((unsigned)ka < nt_lane, ka);
             s.reduce_if<1>((unsigned)kb < nt_lane, kb);
         }
