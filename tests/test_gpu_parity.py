@@ -591,3 +591,29 @@ def test_overwrite_out_device_pointers(c1):
                                    ovw.data_ptr(), overwrite_out=True)
         torch.cuda.synchronize(dev)
     assert torch.equal(acc, ovw)
+
+
+@pytest.mark.parametrize("name,cfg,count,pix_step", [
+    ("config4 bench batch", H.config4, 1024, 64),
+    ("config2 full bunch", H.config2, 10000, 64),
+])
+def test_headline_scale_against_oracle(name, cfg, count, pix_step):
+    """At the headline sizes: the 1024-particle batch of the 1e5-particle
+    bench screen on every 64th of its 40 000 pixels (1.6e9 evaluations), and
+    the full 1e4-particle bunch on every 64th of its 4096 pixels, against the
+    CPU oracle (OpenMP on the host cores), through the automatic kernel choice
+    with host buffers -- the call a drop-in user makes."""
+    w = cfg(count=count)
+    w = w.pixel_subset(np.arange(0, w.n_pix, pix_step))
+    ref, rc = lw.integrate_screen(w.traj, w.pix_pos, w.pix_t0, w.dt, w.nots)
+    assert rc == 0 and np.abs(ref).max() > 0
+    with abi.TrajSet(w.traj) as ts:
+        g = ts.integrate_screen(w.pix_pos, w.pix_t0, w.dt, w.nots)
+        inwin, _, st = ts.last_inwindow()
+    assert st == 0 and inwin > 0
+    e = rel_l2(g, ref)
+    peak = float(np.abs(g - ref).max() / np.abs(ref).max())
+    print(f"{name}: {w.traj.n_particles} particles x {w.n_pix} px, rel L2 vs oracle {e:.3e}, "
+          f"peak sample {peak:.3e}")
+    assert e < TOL_FP32, e
+    assert peak < 10 * TOL_FP32, peak

@@ -723,9 +723,23 @@ struct PairWalk {
     int npa, npb, npp, n_pts;
 };
 
+// An FP64 arrival resolved for a lane: time and encoded decision.
+struct FtimeResult {
+    double ts;
+    int ex;
+    int pad;
+};
+// The FP64-time mode's per-step exchange: [kind][owner lane], kind 0/1 =
+// points i-1 / i of particle a, 2/3 = of particle b.
+struct FtimeShared {
+    FtimeResult r[4][32];
+};
+struct NoFtimeShared {};
+
 // Shared memory of one block (one warp).
-template <int CS>
+template <int CS, bool EXACT = false>
 struct PairSharedT {
+    std::conditional_t<EXACT, FtimeShared, NoFtimeShared> ft;
     PairChunkT<CS> buf[2];
     PixelCtx px[kPThreads];
     PairWalk walk;
@@ -739,7 +753,7 @@ struct PairSharedT {
 template <bool PINGPONG, bool MULTI, bool REC, bool EXACT = false, int CS = kPChunkShift>
 __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc,
                                           const DevWork& wk, int slot, int tile,
-                                          PairSharedT<CS>& sh) {
+                                          PairSharedT<CS, EXACT>& sh) {
     constexpr int kPChunkLen = 1 << CS;
     using PairChunk = PairChunkT<CS>;
     const int pix = tile * kPThreads + threadIdx.x;
@@ -844,24 +858,6 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             atomicAdd(&sh.stats[1], 1ull);
         };
 
-        // The FP64-time mode: point i of particle w resolved with the
-        // reference's arrival time (exa/exb then hold its encoded bin and
-        // flags; 0 = not resolved), and the step from q1 deposited on it.
-        auto ftime_point = [&](auto& q, int w, int i) {
-            const double ts = exact_retarded_time(w ? W.txb[i] : W.txa[i], px.P);
-            const int ex = rec_encode(exact_bin(ts, px.w), exact_flags(ts, px.w));
-            if (w) {
-                q.tsb = ts;
-                q.exb = ex;
-            } else {
-                q.tsa = ts;
-                q.exa = ex;
-            }
-            if constexpr (REC) {
-                if (w) record_point<1>(wk, tr.n_particles, pix, mb, i, q, 0, nt);
-                else record_point<0>(wk, tr.n_particles, pix, ma, i, q, 0, nt);
-            }
-        };
         // Only steps that can reach the window resolve their points: the
         // FP32 chain places every point within chain_err (a few 1e-5) of its
         // bin coordinate, so a point whose chained bin is <= -2 lies before
@@ -869,16 +865,72 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
         // tmax (edge nt - 1/2).  A step ending before the window or starting
         // after it deposits nothing (src/particle.cpp:793), and the
         // accumulator is then empty: arrivals increase along the walk.
-        auto ftime_step = [&](auto wtag, auto& q1, auto& q2, int i) {
+        auto ftime_needed = [&](auto wtag, const auto& q1, const auto& q2, int i) {
             constexpr int Wp = decltype(wtag)::value;
+            if (i > (Wp ? lim_b : lim_a)) return false;
             const int k1 = Wp ? A.Bb + q1.kb : A.Ba + q1.ka;
             const int k2 = Wp ? A.Bb + q2.kb : A.Ba + q2.ka;
             const bool sure = (Wp ? chain_err.v.y : chain_err.v.x) < 0.25f &&
                               fabsf(Wp ? q1.r.v.y : q1.r.v.x) <= 0.5f &&
                               fabsf(Wp ? q2.r.v.y : q2.r.v.x) <= 0.5f;
-            if (sure && (k2 <= -2 || k1 >= nt + 1)) return;
-            if (!(Wp ? q1.exb : q1.exa)) ftime_point(q1, Wp, i - 1);
-            ftime_point(q2, Wp, i);
+            return !(sure && (k2 <= -2 || k1 >= nt + 1));
+        };
+        // The FP64 evaluations the lanes need at this step (point i-1 of a
+        // particle whose window opens here, point i of each particle whose
+        // step can deposit), spread over the warp's lanes: an FP64
+        // instruction costs the pipe as much for one active lane as for 32,
+        // and most lanes need none at most steps.  Lane j evaluates the j-th
+        // request (pixel from the shared pixel data, point from the
+        // trajectory) and the owner takes the result from shared memory.
+        auto ftime_resolve = [&](auto& q1, auto& q2, bool need_a, bool need_b, int i) {
+            if constexpr (EXACT) {
+                const bool lazy_a = need_a && !q1.exa, lazy_b = need_b && !q1.exb;
+                unsigned m[4];
+                m[0] = __ballot_sync(0xffffffffu, lazy_a);
+                m[1] = __ballot_sync(0xffffffffu, need_a);
+                m[2] = __ballot_sync(0xffffffffu, lazy_b);
+                m[3] = __ballot_sync(0xffffffffu, need_b);
+                const int c0 = __popc(m[0]), c1 = c0 + __popc(m[1]), c2 = c1 + __popc(m[2]);
+                const int n = c2 + __popc(m[3]);
+                for (int j = lane; j - lane < n; j += 32) {
+                    if (j < n) {
+                        const int kind = (j >= c0) + (j >= c1) + (j >= c2);
+                        const int base = kind == 0 ? 0 : kind == 1 ? c0 : kind == 2 ? c1 : c2;
+                        const int owner = (int)__fns(m[kind], 0, j - base + 1) & 31;
+                        const PixelCtx& po = sh.px[owner];
+                        const double ts = exact_retarded_time(
+                            (kind < 2 ? W.txa : W.txb)[i - 1 + (kind & 1)], po.P);
+                        FtimeResult& res = sh.ft.r[kind][owner];
+                        res.ts = ts;
+                        res.ex = rec_encode(exact_bin(ts, po.w), exact_flags(ts, po.w));
+                    }
+                }
+                if (n == 0) return;
+                __syncwarp();
+                auto take = [&](auto& q, int w, int kind, int ip) {
+                    const FtimeResult& res = sh.ft.r[kind][lane];
+                    if (w) {
+                        q.tsb = res.ts;
+                        q.exb = res.ex;
+                    } else {
+                        q.tsa = res.ts;
+                        q.exa = res.ex;
+                    }
+                    if constexpr (REC) {
+                        if (w) record_point<1>(wk, tr.n_particles, pix, mb, ip, q, 0, nt);
+                        else record_point<0>(wk, tr.n_particles, pix, ma, ip, q, 0, nt);
+                    }
+                };
+                if (lazy_a) take(q1, 0, 0, i - 1);
+                if (need_a) take(q2, 0, 1, i);
+                if (lazy_b) take(q1, 1, 2, i - 1);
+                if (need_b) take(q2, 1, 3, i);
+                __syncwarp();  // the exchange is reused at the next step
+            }
+        };
+        // The step q1 -> q2 of particle Wp with both points resolved.
+        auto ftime_step = [&](auto wtag, auto& q1, auto& q2, int i) {
+            constexpr int Wp = decltype(wtag)::value;
             const int e1 = Wp ? q1.exb : q1.exa, e2 = Wp ? q2.exb : q2.exa;
             const int idx1 = (e1 & ((1 << kRecFlagShift) - 1)) - 4;
             const int idx2 = (e2 & ((1 << kRecFlagShift) - 1)) - 4;
@@ -924,8 +976,11 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             if constexpr (EXACT) {
                 // FP32 fields, the reference's FP64 arrival times: the bin and
                 // flags of every point that can deposit are the reference's
-                if (i <= lim_a) ftime_step(kPa, q1, q2, i);
-                if (i <= lim_b) ftime_step(kPb, q1, q2, i);
+                const bool need_a = ftime_needed(kPa, q1, q2, i);
+                const bool need_b = ftime_needed(kPb, q1, q2, i);
+                ftime_resolve(q1, q2, need_a, need_b, i);
+                if (need_a) ftime_step(kPa, q1, q2, i);
+                if (need_b) ftime_step(kPb, q1, q2, i);
                 return;
             }
             // the step ending at point i belongs to this lane and slot
@@ -1159,7 +1214,7 @@ template <int MAXREG, bool PINGPONG, bool MULTI = false, bool REC = false, bool 
           int CS = kPChunkShift>
 __global__ void __maxnreg__(MAXREG)
     lw_fp32_pair_kernel(DevTraj tr, DevScreen sc, DevWork wk) {
-    __shared__ PairSharedT<CS> sh;
+    __shared__ PairSharedT<CS, EXACT> sh;
     pair_tile<PINGPONG, MULTI, REC, EXACT, CS>(tr, sc, wk, blockIdx.y, blockIdx.x, sh);
 }
 
