@@ -379,6 +379,16 @@ int teufel_cuda_last_timing(const teufel_traj_set *traj, int64_t *deposits,
  * FP32 (fma.rn.f32x2) and FP64 (DFMA).  Any pointer may be NULL. */
 int teufel_cuda_probe_peaks(double *fp32_tflops, double *fp32x2_tflops, double *fp64_tflops);
 
+/* Diagnostic for the tests: the FP64-time mode's quotients against the IEEE
+ * division on the device.  For i < n: q[2i] = a[i]/b as that mode forms it
+ * (a product with RN(1/b), one FMA correction, the IEEE division where the
+ * correction cannot prove the rounded quotient), q[2i+1] = the IEEE a[i]/b;
+ * k[2i] = the bin round((ts[i] - t0)/dt) clamped to [-2, nt+1] as that mode
+ * forms it (a product with RN(1/dt)), k[2i+1] = the same with the IEEE
+ * quotient (the reference's).  Host pointers; dt > 0. */
+int teufel_cuda_check_fixed_division(int n, const double *a, double b, const double *ts,
+                                     double t0, double dt, int nt, double *q, int32_t *k);
+
 #ifdef __cplusplus
 }
 #endif

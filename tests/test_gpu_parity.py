@@ -617,3 +617,29 @@ def test_headline_scale_against_oracle(name, cfg, count, pix_step):
           f"peak sample {peak:.3e}")
     assert e < TOL_FP32, e
     assert peak < 10 * TOL_FP32, peak
+
+
+def test_fp64_time_quotients_equal_ieee_division():
+    """The FP64-time mode forms R/c and the bin round((ts - t0)/dt) with a
+    product by the reciprocal, one FMA correction and a residual test that
+    falls back to the IEEE division; every result must be the IEEE one, bit
+    for bit: distances of a screen 1-40 m away, random and next to rounding
+    ties of the quotient, and arrival times over a 8192-bin window including
+    half-integer bin coordinates (ties of round()) and points far outside."""
+    rng = np.random.default_rng(17)
+    C = 2.99792458e8
+    n = 1 << 20
+    R = rng.uniform(1.0, 40.0, n)
+    # distances whose quotient by c sits next to a rounding tie: q + ulp/2
+    q = R[: n // 4] / C
+    R[: n // 4] = (q + np.spacing(q) * 0.5) * C
+    R[n // 8: n // 4] = np.nextafter(R[n // 8: n // 4], np.inf)
+    t0, dt, nt = 1.0000512e-7, 1e-18, 8192
+    u = np.concatenate([rng.uniform(-20, nt + 20, n // 2),
+                        np.round(rng.uniform(-4, nt + 4, n // 4)) + 0.5,
+                        rng.uniform(-1e7, 1e7, n // 4)])
+    ts = t0 + u * dt
+    qq, kk = abi.check_fixed_division(R, C, ts, t0, dt, nt)
+    assert np.array_equal(qq[:, 0].view(np.int64), qq[:, 1].view(np.int64))
+    assert np.array_equal(kk[:, 0], kk[:, 1])
+    assert np.array_equal(qq[:, 1], R / C)  # the IEEE quotient, as numpy forms it

@@ -38,7 +38,7 @@ EXPORTED = [
     "teufel_cuda_batch_create", "teufel_cuda_batch_run", "teufel_cuda_batch_status",
     "teufel_cuda_batch_free", "teufel_cuda_autotune", "teufel_cuda_retarded_field",
     "teufel_cuda_traj_track", "teufel_cuda_traj_download", "teufel_cuda_record_decisions",
-    "teufel_cuda_batch_record_decisions",
+    "teufel_cuda_batch_record_decisions", "teufel_cuda_check_fixed_division",
 ]
 
 # bytes of the fixed device array used by teufel_cuda_integrate_screen_noalloc
@@ -140,6 +140,10 @@ def lib():
                                                            ctypes.c_int, ctypes.c_int, _vp, _vp]
         L.teufel_cuda_probe_peaks.restype = ctypes.c_int
         L.teufel_cuda_probe_peaks.argtypes = [_dp, _dp, _dp]
+        L.teufel_cuda_check_fixed_division.restype = ctypes.c_int
+        L.teufel_cuda_check_fixed_division.argtypes = [
+            ctypes.c_int, _dp, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_double,
+            ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_int32)]
         L.teufel_cuda_batch_create.restype = ctypes.c_int
         L.teufel_cuda_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(ObserverDesc),
                                                ctypes.POINTER(Options),
@@ -419,6 +423,21 @@ def deposit_injected(ts_list, f_list, t0, dt, nots, precision=PREC_FP64, trace=N
     st = lib().teufel_cuda_deposit_injected(len(ts_list), _ptr(n_points, _ip), _ptr(ts), _ptr(f),
                                             t0, dt, nots, precision, _ptr(trace))
     return trace, st
+
+
+def check_fixed_division(a, b, ts, t0, dt, nt):
+    """teufel_cuda_check_fixed_division: (quotients [n][2], bins [n][2]) --
+    the FP64-time mode's a/b and bin of ts, and the IEEE ones."""
+    a = _c(a).reshape(-1)
+    ts = _c(ts).reshape(-1)
+    assert a.shape == ts.shape
+    n = a.shape[0]
+    q = np.zeros((n, 2))
+    k = np.zeros((n, 2), dtype=np.int32)
+    check(lib().teufel_cuda_check_fixed_division(n, _ptr(a), b, _ptr(ts), t0, dt, nt, _ptr(q),
+                                                 _ptr(k, ctypes.POINTER(ctypes.c_int32))),
+          "teufel_cuda_check_fixed_division")
+    return q, k
 
 
 def probe_peaks():

@@ -52,6 +52,41 @@ __device__ __forceinline__ double exact_retarded_time(const double4_32a tx, cons
     return __dadd_rn(tx.x, __ddiv_rn(R, kC));
 }
 
+// a / b rounded to nearest for a divisor with a known reciprocal y = RN(1/b),
+// in fewer FP64 operations than the IEEE division: q0 = RN(a y) lies within
+// two ulps of a/b, the residual a - q0 b is formed by an FMA, and one
+// correction step q1 = RN(q0 + r y) (Markstein's, 1990) gives the rounded
+// quotient in all but rare cases.  q1 is returned only when its own residual
+// proves it: a - q1 b is exact in an FMA for a q1 next to a/b, and
+// |a - q1 b| < |b| ulp(q1)/2 (1 - 2^-20) puts a/b strictly within half a
+// spacing of q1 on both sides (q1 not a power of two, whose lower spacing is
+// half as wide).  Otherwise -- near a rounding tie, subnormal, huge or
+// non-finite values -- the IEEE division decides.
+__device__ __forceinline__ double div_rn_by(double a, double b, double y) {
+    const double q0 = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-q0, b, a), y, q0);
+    const double r1 = __fma_rn(-q1, b, a);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(q1);
+    const unsigned long long ex = bits & 0x7ff0000000000000ULL;
+    // ulp(q1) = 2^(e - 52) for exponent fields e in (53, 2047)
+    if (ex > (53ULL << 52) && ex < 0x7ff0000000000000ULL && (bits & 0x000fffffffffffffULL)) {
+        const double ulp = __longlong_as_double((long long)(ex - (52ULL << 52)));
+        if (fabs(r1) < fabs(b) * ulp * (0.5 * (1.0 - 0x1p-20))) return q1;
+    }
+    return __ddiv_rn(a, b);
+}
+
+// exact_retarded_time with R/c through div_rn_by: the same double.
+__device__ __forceinline__ double exact_retarded_time_fast(const double4_32a tx,
+                                                           const double3 obs) {
+    double rx = __dsub_rn(obs.x, tx.y);
+    double ry = __dsub_rn(obs.y, tx.z);
+    double rz = __dsub_rn(obs.z, tx.w);
+    double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+    double R = __dsqrt_rn(r2);
+    return __dadd_rn(tx.x, div_rn_by(R, kC, 1.0 / kC));
+}
+
 // Bin index of an exact arrival time, clamped to [-2, nt+1].  The clamp keeps
 // every decision the deposit takes (indices below 0 only matter through the
 // tmin flag, indices above nt are capped to nt by the reference, :806, :834).
@@ -60,6 +95,20 @@ __device__ __forceinline__ int exact_bin(double ts, const Window& w) {
     u = fmax(-4.0, fmin(u, (double)w.nt + 4.0));
     int k = (int)round(u);  // round(): half away from zero, as C's round()
     return k < -2 ? -2 : (k > w.nt + 1 ? w.nt + 1 : k);
+}
+
+// exact_bin with the quotient replaced by a product with inv_dt = RN(1/dt):
+// the two differ by at most two ulps, so they round to the same integer
+// unless the product lies within 1e-9 of a half-integer (then the IEEE
+// quotient decides).  The same bin for |(ts - t0)/dt| < 2^20.
+__device__ __forceinline__ int exact_bin_fast(double ts, const Window& w, double inv_dt) {
+    const double d = __dsub_rn(ts, w.t0);
+    double u = __dmul_rn(d, inv_dt);
+    const double k = round(u);
+    if (!(fabs(u - k) < 0.5 - 1e-9) || !(fabs(u) < 1048576.0)) u = __ddiv_rn(d, w.dt);
+    u = fmax(-4.0, fmin(u, (double)w.nt + 4.0));
+    const int ki = (int)round(u);
+    return ki < -2 ? -2 : (ki > w.nt + 1 ? w.nt + 1 : ki);
 }
 
 __device__ __forceinline__ int exact_flags(double ts, const Window& w) {

@@ -898,11 +898,12 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                         const int base = kind == 0 ? 0 : kind == 1 ? c0 : kind == 2 ? c1 : c2;
                         const int owner = (int)__fns(m[kind], 0, j - base + 1) & 31;
                         const PixelCtx& po = sh.px[owner];
-                        const double ts = exact_retarded_time(
+                        const double ts = exact_retarded_time_fast(
                             (kind < 2 ? W.txa : W.txb)[i - 1 + (kind & 1)], po.P);
                         FtimeResult& res = sh.ft.r[kind][owner];
                         res.ts = ts;
-                        res.ex = rec_encode(exact_bin(ts, po.w), exact_flags(ts, po.w));
+                        res.ex = rec_encode(exact_bin_fast(ts, po.w, po.inv_dt),
+                                            exact_flags(ts, po.w));
                     }
                 }
                 if (n == 0) return;

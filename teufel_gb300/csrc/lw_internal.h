@@ -178,6 +178,8 @@ cudaError_t launch_deposit_injected32(int n_part, const int64_t* offs, const dou
                                       double* trace, float* trace32, unsigned int* status,
                                       cudaStream_t s);
 int probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops);
+int fixed_division_check(int n, const double* a, double b, const double* ts, double t0,
+                         double dt, int nt, double* q, int* k);
 
 // The lattice the device pusher tracks through (lw_track.cu): a planar
 // undulator centred at `origin` and a homogeneous field; kz = 2 pi / lambda_u.

@@ -290,6 +290,43 @@ static double time_probe_f32x2(int iters, int blocks, int threads) {
     return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
 }
 
+// The FP64-time mode's quotients (R/c, the bin of an arrival time) against
+// the IEEE division, element by element.
+__global__ void fixed_division_check_kernel(int n, const double* a, double b, const double* ts,
+                                            double t0, double dt, int nt, double* q, int* k) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Window w = make_window(t0, dt, nt);
+    q[2 * i] = div_rn_by(a[i], b, 1.0 / b);
+    q[2 * i + 1] = __ddiv_rn(a[i], b);
+    k[2 * i] = exact_bin_fast(ts[i], w, 1.0 / w.dt);
+    k[2 * i + 1] = exact_bin(ts[i], w);
+}
+
+int fixed_division_check(int n, const double* a, double b, const double* ts, double t0,
+                         double dt, int nt, double* q, int* k) {
+    double *d_a = nullptr, *d_ts = nullptr, *d_q = nullptr;
+    int* d_k = nullptr;
+    cudaError_t e = cudaMalloc(&d_a, sizeof(double) * n);
+    if (!e) e = cudaMalloc(&d_ts, sizeof(double) * n);
+    if (!e) e = cudaMalloc(&d_q, sizeof(double) * 2 * n);
+    if (!e) e = cudaMalloc(&d_k, sizeof(int) * 2 * n);
+    if (!e) e = cudaMemcpy(d_a, a, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_ts, ts, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (!e) {
+        fixed_division_check_kernel<<<(n + 255) / 256, 256>>>(n, d_a, b, d_ts, t0, dt, nt, d_q,
+                                                              d_k);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpy(q, d_q, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(k, d_k, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost);
+    cudaFree(d_a);
+    cudaFree(d_ts);
+    cudaFree(d_q);
+    cudaFree(d_k);
+    return e == cudaSuccess ? 0 : 1;
+}
+
 int probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* fp64_tflops) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);

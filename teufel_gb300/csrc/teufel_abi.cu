@@ -1302,4 +1302,14 @@ int teufel_cuda_probe_peaks(double* fp32_tflops, double* fp32x2_tflops, double* 
     return probe_peaks(fp32_tflops, fp32x2_tflops, fp64_tflops) ? TEUFEL_ERR_CUDA : TEUFEL_OK;
 }
 
+int teufel_cuda_check_fixed_division(int n, const double* a, double b, const double* ts,
+                                     double t0, double dt, int nt, double* q, int* k) {
+    if (n < 0 || (n > 0 && (!a || !ts || !q || !k)) || !(dt > 0.0) || nt < 0)
+        return TEUFEL_ERR_ARG;
+    int rc = check_device();
+    if (rc) return rc;
+    if (n == 0) return TEUFEL_OK;
+    return fixed_division_check(n, a, b, ts, t0, dt, nt, q, k) ? TEUFEL_ERR_CUDA : TEUFEL_OK;
+}
+
 }  // extern "C"
