@@ -263,7 +263,11 @@ typedef struct teufel_batch teufel_batch;
  * CUDA graph, which teufel_cuda_batch_run replays.  Observers may share a
  * trajectory set.  opt: precision must be TEUFEL_PREC_FP32_SPLIT;
  * device_pointers must be 1; n_slots (0 = automatic) caps the particle
- * ranges per observer.  The trajectory sets and device arrays must outlive
+ * ranges per observer.  A batch always uses the chained FP32 arrival times:
+ * an observer whose bins are short against FP64's rounding of its arrival
+ * times (where teufel_cuda_integrate_screen switches to
+ * TEUFEL_PREC_FP32_FP64TIME) gets traces closer to the exact arrival times
+ * than the FP64 reference's, which differ from them at that rounding.  The trajectory sets and device arrays must outlive
  * the batch. */
 int teufel_cuda_batch_create(int n_obs, const teufel_observer *obs, const teufel_options *opt,
                              teufel_batch **out);
