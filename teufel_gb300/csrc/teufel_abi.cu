@@ -321,7 +321,7 @@ bool needs_fp64_time(double max_abs_t0, double dt) {
 int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, double dt, int nt,
                int np, double* d_out, const teufel_options& opt_in, cudaStream_t s,
                int slot_pct = 100, const HostOut* ho = nullptr, int* d_rec = nullptr,
-               size_t staged_bytes = 0) {
+               size_t staged_bytes = 0, double t0max_known = -1.0) {
     teufel_options opt = opt_in;
     // dt < 0 reverses the reference's window (tmin = t0 - dt/2 > tmax): a
     // step then deposits only when its arrivals straddle that window, and
@@ -336,9 +336,12 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
     if (!fp64 && opt.kernel_variant == 0) {
         // automatic: the FP64-time mode where FP64's rounding of the arrival
         // times is not negligible against the bins
-        double t0max = 0.0;
-        int rc = max_abs_t0(h, d_t0, np, s, &t0max);
-        if (rc) return rc;
+        // (known on the host for host-buffer calls; else a device reduction)
+        double t0max = t0max_known;
+        if (!(t0max >= 0.0)) {
+            int rc = max_abs_t0(h, d_t0, np, s, &t0max);
+            if (rc) return rc;
+        }
         if (needs_fp64_time(t0max, dt)) opt.kernel_variant = 9;
     }
     if (!fp64 && opt.kernel_variant == 0) {
@@ -933,6 +936,8 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
         return run_device(h, pix_pos, pix_t0, dt, Nt, Np, out, opt, s);
     }
     if (!finite_array(pix_pos, 3 * (int64_t)Np) || !finite_array(pix_t0, Np)) return TEUFEL_ERR_ARG;
+    double t0max = 0.0;
+    for (int p = 0; p < Np; p++) t0max = std::max(t0max, std::fabs(pix_t0[p]));
     const size_t nout = (size_t)Np * (size_t)Nt * 6;
     // the staged pixel and trace buffers count against the caller's bound
     const size_t staged = sizeof(double) * (4 * (size_t)Np + nout);
@@ -964,7 +969,8 @@ int teufel_cuda_integrate_screen_ex(const teufel_traj_set* traj_c, const double*
                                  h->copy_s));
     TRY_CUDA(cudaEventRecord(h->cev[1], h->copy_s));
     const HostOut ho{out, h->copy_s, h->cev[1], h->cev.data() + 3, kOutChunks};
-    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s, 100, &ho, nullptr, staged);
+    rc = run_device(h, d_pos, d_t0, dt, Nt, Np, h->d_out, opt, s, 100, &ho, nullptr, staged,
+                    t0max);
     if (rc) {
         cudaStreamSynchronize(h->copy_s);
         cudaStreamSynchronize(s);
