@@ -299,9 +299,9 @@ class TrajSet:
         pix_t0 = _c(pix_t0).reshape(-1)
         n_pix = pix_pos.shape[0]
         if out is None:
-            # a new buffer receives the traces: nothing to clear or upload
-            out = np.empty((n_pix, nots, 6))
-            overwrite_out = True
+            # zeros, not an unwritten buffer: copying the traces back into
+            # pages the process has never touched runs at a few GB/s
+            out = np.zeros((n_pix, nots, 6))
         if not (out.dtype == np.float64 and out.flags.c_contiguous):
             raise ValueError("out must be a C-contiguous float64 array")
         opt = options(precision, False, n_slots, variant=variant, max_device_mib=max_device_mib,
