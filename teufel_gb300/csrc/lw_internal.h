@@ -113,6 +113,10 @@ struct DevWork {
     // 1: the reduction stores the traces into out (out treated as zero)
     // instead of adding them
     int overwrite;
+    // 1: the reduction clears the partial traces it has read, for a next use
+    // of the memory without a memset (the batch's graph replays); 0: the
+    // caller clears them before their next use
+    int clear;
 };
 
 // A point decision as recorded: bin index + 4 in bits 0-26, the window and

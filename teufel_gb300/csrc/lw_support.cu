@@ -33,12 +33,14 @@ __device__ __forceinline__ void reduce_fp32_bin(const DevWork& w, int64_t e, dou
         kahan(4, c.x);
         kahan(5, c.y);
     }
-    const float2 z = make_float2(0.0f, 0.0f);
-    for (int s = 0; s < w.n_slots; s++) {
-        float2* p = (float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
-        __stcs(p, z);
-        __stcs(p + 1, z);
-        __stcs(p + 2, z);
+    if (w.clear) {
+        const float2 z = make_float2(0.0f, 0.0f);
+        for (int s = 0; s < w.n_slots; s++) {
+            float2* p = (float2*)(scr + (int64_t)s * w.slot_stride + e * 6);
+            __stcs(p, z);
+            __stcs(p + 1, z);
+            __stcs(p + 2, z);
+        }
     }
     double acc[6];
 #pragma unroll
@@ -110,12 +112,14 @@ __global__ void reduce_fp64_kernel(DevWork w, int64_t e0, int64_t e1, double* ou
             acc[4] += c.x;
             acc[5] += c.y;
         }
-        const double2 z = make_double2(0.0, 0.0);
-        for (int s = 0; s < w.n_slots; s++) {
-            double2* p = (double2*)(scr + (int64_t)s * w.slot_stride + e * 6);
-            __stcs(p, z);
-            __stcs(p + 1, z);
-            __stcs(p + 2, z);
+        if (w.clear) {
+            const double2 z = make_double2(0.0, 0.0);
+            for (int s = 0; s < w.n_slots; s++) {
+                double2* p = (double2*)(scr + (int64_t)s * w.slot_stride + e * 6);
+                __stcs(p, z);
+                __stcs(p + 1, z);
+                __stcs(p + 2, z);
+            }
         }
         double* o = out + e * 6;
 #pragma unroll

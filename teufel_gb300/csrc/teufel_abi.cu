@@ -404,7 +404,6 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         cudaStream_t s;
         ~Release() { cudaFreeAsync(p, s); }
     } release{scratch, s};
-    TRY_CUDA(cudaMemsetAsync(scratch, 0, scratch_bytes, s));
     h->last_slots = (int)slots_total;
     // geometric slot sizes for the pair kernel's grids of three waves or more
     // (below that the longest blocks set the time, and equal slots are best)
@@ -447,6 +446,9 @@ int run_device(teufel_traj_set* h, const double* d_pos, const double* d_t0, doub
         w.slot_seg = h->slot_seg + p0;
         w.scratch = scratch;
         w.slot_stride = (int64_t)np * nt * 6;
+        // the slots this pass accumulates into start from zero; the reduction
+        // leaves them as they are
+        TRY_CUDA(cudaMemsetAsync(scratch, 0, slot_bytes * (size_t)w.n_slots, s));
         w.status = h->d_status;
         w.frame = h->dev.frame;
         w.counters = h->d_counters;

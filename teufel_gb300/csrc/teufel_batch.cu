@@ -204,6 +204,7 @@ int teufel_cuda_batch_create(int n_obs, const teufel_observer* obs, const teufel
         w.slot_stride = (int64_t)ob.Np * ob.Nt * 6;
         w.status = b->d_status;
         w.counters = b->d_counters;
+        w.clear = 1;  // cleared at creation, and by each replay's reduction
         scratch_off += (size_t)p.slots * (size_t)w.slot_stride;
         h_wk[k] = w;
         h_out[k] = ob.out;
