@@ -8,7 +8,7 @@
 namespace teufel {
 
 // out[e] += the sum over slots of the FP32 partial traces of bin e (B from
-// cB), and the partial traces cleared for the next use.  The slots are summed
+// cB), and (w.clear) the partial traces cleared for their next use.  The slots are summed
 // in slot order in FP32 with Kahan compensation (on the FP32 pipe: FP64 runs at
 // 1/64 of its rate here), and each component enters FP64 once, as its sum
 // plus compensation; the error of the sum is a few FP32 ulps of the smallest
