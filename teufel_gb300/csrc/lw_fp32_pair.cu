@@ -989,24 +989,32 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             const int2 nr = near(q2);
             const int k1a = A.Ba + q1.ka, k1b = A.Bb + q1.kb;
             const int k2a = A.Ba + q2.ka, k2b = A.Bb + q2.kb;
-            // regular: resolved without the fallback, bin inside the trace
-            const bool r1a = q1.exa == 0 && (unsigned)k1a < (unsigned)nt;
-            const bool r1b = q1.exb == 0 && (unsigned)k1b < (unsigned)nt;
-            const bool r2a = !nr.x && (unsigned)k2a < (unsigned)nt;
-            const bool r2b = !nr.y && (unsigned)k2b < (unsigned)nt;
-            const bool fast_a = r1a && r2a && (unsigned)(q2.ka - q1.ka) <= 1u;
-            const bool fast_b = r1b && r2b && (unsigned)(q2.kb - q1.kb) <= 1u;
-            // certainly outside the window: adds nothing
-            const bool out_a = (!nr.x && k2a < 0) || (q1.exa == 0 && k1a >= nt);
-            const bool out_b = (!nr.y && k2b < 0) || (q1.exb == 0 && k1b >= nt);
-            const bool ok_a = !dep_a || (!nr.x && (fast_a || out_a));
-            const bool ok_b = !dep_b || (!nr.y && (fast_b || out_b));
+            // Regular: resolved without the fallback, advancing by at most one
+            // bin.  Wherever such a step lies, the fast deposit is the
+            // reference's: inside the window; entering it (bin -1 to 0) it puts
+            // into bin 0 the part after the edge, as the reference's branch for
+            // a step that starts before the window does; leaving it (bin nt-1
+            // to nt) it puts into bin nt-1 the part before the edge (the
+            // reference caps the last bin at nt and adds nothing there); and
+            // what falls in bins outside [0, nt) stays in the accumulator, which
+            // is never added to the trace for such a bin.
+            const bool fast_a = q1.exa == 0 && !nr.x && (unsigned)(q2.ka - q1.ka) <= 1u;
+            const bool fast_b = q1.exb == 0 && !nr.y && (unsigned)(q2.kb - q1.kb) <= 1u;
+            const bool ok_a = !dep_a || fast_a;
+            const bool ok_b = !dep_b || fast_b;
             const bool ca = q2.ka != q1.ka, cb = q2.kb != q1.kb;
             const bool v1a = (unsigned)k1a < nt_lane, v1b = (unsigned)k1b < nt_lane;
             bool go_multi = false;
             bool multi_a = false, multi_b = false;
             const bool go_fast = __all_sync(0xffffffffu, ok_a && ok_b);
             if constexpr (MULTI) {
+                // bins inside the trace, or certainly outside the window
+                const bool r1a = q1.exa == 0 && (unsigned)k1a < (unsigned)nt;
+                const bool r1b = q1.exb == 0 && (unsigned)k1b < (unsigned)nt;
+                const bool r2a = !nr.x && (unsigned)k2a < (unsigned)nt;
+                const bool r2b = !nr.y && (unsigned)k2b < (unsigned)nt;
+                const bool out_a = (!nr.x && k2a < 0) || (q1.exa == 0 && k1a >= nt);
+                const bool out_b = (!nr.y && k2b < 0) || (q1.exb == 0 && k1b >= nt);
                 multi_a = r1a && r2a && (unsigned)(q2.ka - q1.ka) <= (unsigned)kMaxSpan;
                 multi_b = r1b && r2b && (unsigned)(q2.kb - q1.kb) <= (unsigned)kMaxSpan;
                 if (!go_fast)
@@ -1017,8 +1025,16 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             if (go_fast) {
                 const bool da = dep_a && fast_a, db = dep_b && fast_b;
                 deposit_fast2(q1, q2, da, db, ca, cb, k1a, k1b, v1a, v1b, s);
-                inwin += (unsigned)da + (unsigned)db;
-                n_add += (unsigned)da + (unsigned)db + (unsigned)(da && ca) + (unsigned)(db && cb);
+                // the steps the reference deposits (ts2 > tmin, ts1 < tmax), and
+                // the bins inside the trace they add to
+                const bool ia = da && k2a >= 0 && k1a < nt, ib = db && k2b >= 0 && k1b < nt;
+                inwin += (unsigned)ia + (unsigned)ib;
+                n_add += (ia ? (unsigned)((unsigned)k1a < (unsigned)nt) +
+                                   (unsigned)(ca && (unsigned)k2a < (unsigned)nt)
+                             : 0u) +
+                         (ib ? (unsigned)((unsigned)k1b < (unsigned)nt) +
+                                   (unsigned)(cb && (unsigned)k2b < (unsigned)nt)
+                             : 0u);
             } else if (go_multi) {
                 const bool da = dep_a && multi_a, db = dep_b && multi_b;
                 deposit_multi2(q1, q2, da, db, ca, cb, k1a, k1b, v1a, v1b, s);
