@@ -12,12 +12,17 @@
 // Bin decisions, fallbacks and the sink stay per particle.
 //
 // The step loop has one warp vote per step.  When every lane's steps are
-// regular (both points resolved without the exact fallback, inside the trace,
-// advancing by 0 or 1 bin) or certainly outside the window, the warp deposits
-// them on a straight-line path without branches; anything else -- a point
-// within its error bound of a bin edge, a step at the window's edge or one
-// that spans several bins -- takes the general path, which is the reference's
-// full case analysis (src/particle.cpp:786-865).
+// regular (both points resolved without the exact fallback, advancing by 0 or
+// 1 bin, wherever they lie against the window), the warp deposits them on a
+// straight-line path without branches; anything else -- a point within its
+// error bound of a bin edge, or a step that spans several bins -- takes the
+// general path, which is the reference's full case analysis
+// (src/particle.cpp:786-865).
+//
+// The FP64-time instantiation (EXACT) takes the reference's FP64 arrival
+// times, bins and bin edges for every point that can deposit, evaluated by
+// the lanes of the warp in turn (ftime_resolve), with the FP32 chain deciding
+// which points can.
 //
 // Each particle's open bin is implicit: the register accumulator of a
 // particle always holds the not-yet-added contribution to the bin of its
