@@ -385,13 +385,13 @@ struct GeneralSink {
     int open;
     int nt;
     unsigned int* err;
-    unsigned int* n_add;
+    unsigned int* n_add;  // counts the contributions; nullptr: not counted here
     __device__ __forceinline__ void add(int k, const float2* f) {
         if (k < 0 || k >= nt) {
             *err |= 1u << TEUFEL_ERR_RANGE;
             return;
         }
-        (*n_add)++;
+        if (n_add) (*n_add)++;
         if (k == open) {
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -747,6 +747,7 @@ struct PairSharedT {
     std::conditional_t<EXACT, FtimeShared, NoFtimeShared> ft;
     PairChunkT<CS> buf[2];
     PixelCtx px[kPThreads];
+    int2 kstart[kPThreads];  // per lane: the bins (a, b) of the walk's first point
     PairWalk walk;
     unsigned long long stats[2];  // point evaluations, exact fallbacks
     unsigned long long bar[2];    // the buffers' bulk-copy barriers
@@ -1030,29 +1031,21 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
             if (go_fast) {
                 const bool da = dep_a && fast_a, db = dep_b && fast_b;
                 deposit_fast2(q1, q2, da, db, ca, cb, k1a, k1b, v1a, v1b, s);
-                // the steps the reference deposits (ts2 > tmin, ts1 < tmax), and
-                // the bins inside the trace they add to
+                // the steps the reference deposits (ts2 > tmin, ts1 < tmax); the
+                // bins they add to are counted once per walk
                 const bool ia = da && k2a >= 0 && k1a < nt, ib = db && k2b >= 0 && k1b < nt;
                 inwin += (unsigned)ia + (unsigned)ib;
-                n_add += (ia ? (unsigned)((unsigned)k1a < (unsigned)nt) +
-                                   (unsigned)(ca && (unsigned)k2a < (unsigned)nt)
-                             : 0u) +
-                         (ib ? (unsigned)((unsigned)k1b < (unsigned)nt) +
-                                   (unsigned)(cb && (unsigned)k2b < (unsigned)nt)
-                             : 0u);
             } else if (go_multi) {
                 const bool da = dep_a && multi_a, db = dep_b && multi_b;
                 deposit_multi2(q1, q2, da, db, ca, cb, k1a, k1b, v1a, v1b, s);
                 inwin += (unsigned)da + (unsigned)db;
-                n_add += (unsigned)da + (unsigned)db + (unsigned)(da ? q2.ka - q1.ka : 0) +
-                         (unsigned)(db ? q2.kb - q1.kb : 0);
             } else {
                 // the general path: exact fallbacks, then the reference's
                 // deposit per particle through the accumulator of its bin
                 if (dep_a && nr.x) resolve(q2, 0, i);
                 if (dep_b && nr.y) resolve(q2, 1, i);
                 {
-                    GeneralSink<0> g{&s, v1a ? k1a : -1, nt, &err, &n_add};
+                    GeneralSink<0> g{&s, v1a ? k1a : -1, nt, &err, nullptr};
                     if (dep_a) {
                         const PointState u1 = unpack<0>(q1, A.Ba, nt), u2 = unpack<0>(q2, A.Ba, nt);
                         if (deposit_step32(u1, u2, A.Ba, nt, g)) inwin++;
@@ -1063,7 +1056,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                     if (moved) s.clear<0>();
                 }
                 {
-                    GeneralSink<1> g{&s, v1b ? k1b : -1, nt, &err, &n_add};
+                    GeneralSink<1> g{&s, v1b ? k1b : -1, nt, &err, nullptr};
                     if (dep_b) {
                         const PointState u1 = unpack<1>(q1, A.Bb, nt), u2 = unpack<1>(q2, A.Bb, nt);
                         if (deposit_step32(u1, u2, A.Bb, nt, g)) inwin++;
@@ -1146,6 +1139,7 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                     const int2 nr = near(p1);
                     if (nr.x && start <= lim_a) resolve(p1, 0, start);
                     if (nr.y && start <= lim_b) resolve(p1, 1, start);
+                    sh.kstart[threadIdx.x] = make_int2(A.Ba + p1.ka, A.Bb + p1.kb);
                 }
                 if constexpr (REC && !EXACT) {
                     if (start <= lim_a)
@@ -1193,6 +1187,18 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
                                  : A.Bb + p1.kb;
             s.reduce_if<0>((unsigned)ka < nt_lane, ka);
             s.reduce_if<1>((unsigned)kb < nt_lane, kb);
+            if constexpr (!EXACT) {
+                // Bins the walk added to beyond one per in-window step: its
+                // arrivals increase, and every step adds to each bin of the
+                // trace between its end points' bins (the reference's
+                // partial, full and partial bins), so over the walk they are
+                // the bin edges inside the trace crossed between its first
+                // and its last point.  Every point the walk reaches is one of
+                // the particle's steps in this slot, or its repeated last point.
+                const int2 k0 = sh.kstart[threadIdx.x];
+                if (lim_a >= 0) n_add += (unsigned)max(0, min(ka, nt - 1) - max(k0.x, 0));
+                if (lim_b >= 0) n_add += (unsigned)max(0, min(kb, nt - 1) - max(k0.y, 0));
+            }
         }
     }
     if (kBulkStage) {
@@ -1205,7 +1211,8 @@ __device__ __forceinline__ void pair_tile(const DevTraj& tr, const DevScreen& sc
     }
     if (err) atomicOr(wk.status, err);
     const unsigned long long win = warp_sum_u64(inwin);
-    const unsigned long long nadd = warp_sum_u64(n_add);
+    // deposits: per in-window step one bin, plus the edges crossed
+    const unsigned long long nadd = warp_sum_u64(EXACT ? n_add : n_add + inwin);
     __syncwarp();
     if (lane == 0 && wk.counters) {
         if (win) atomicAdd(wk.counters, win);
