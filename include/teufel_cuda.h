@@ -215,7 +215,7 @@ int teufel_cuda_retarded_field(const teufel_traj_set *traj, double obs_time, int
 
 /* No counterpart in the reference.  Tunes the FP32 split-precision path for
  * one observer shape: times the kernel variants (warp-uniform; two particles
- * per thread at 12 to 16 resident warps per SM, at 16 with packed
+ * per thread at 13 to 16 resident warps per SM, at 16 with packed
  * multi-bin deposits, and at 16 with trajectory chunks of 8 and of 32
  * points) at the automatic slot count -- or only the FP64-time
  * kernel (9) where TEUFEL_PREC_FP32_FP64TIME's rule selects it --
